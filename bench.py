@@ -1,0 +1,358 @@
+"""Benchmark: particle-steps/s of the Particle Life physics step at 1M, 2D.
+
+Workload (the reference-units restatement of the 1M 2D configuration):
+2D periodic unit box, N = 1,000,000 particles, 8 types assigned uniformly,
+matrix uniform in [-1,1], positions uniform, velocities zero, rmax = 0.0025
+(0.005 in a [-1,1]^2 box, ~19.6 neighbours), beta = 0.3, friction half-life
+0.043 s (coefficient 0.7644018106552037), dt = 0.01, force 1.  Seeded
+synthetic data (numpy Philox); FP32 state on the GPU.
+
+Our arm (default):
+  value  device-resident state; each step timed alone with CUDA events on the
+         library's stream; L2 flushed (256 MB write) between steps.
+  e2e    the public API with host buffers: per step plg_upload (pinned host
+         double/int arrays) + plg_step + plg_download, host wall clock.
+  roofline of the dominant kernel (the force kernel), from per-kernel CUDA
+         events over a profiled pass of the same steps.
+  cpu_baseline  the oracle (C FP64 restatement of the reference's step, all
+         host threads) on a bounded sample of steps of the same workload.
+--impl reference: the same workload through the oracle port on all host
+cores (the reference is Java and no JDK exists on either machine).
+
+Multi-GPU: replicas only (one world per rank, no collective on the data path);
+value = units of all ranks / max over ranks of the timed region.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+REPO = Path(__file__).resolve().parent
+sys.path.insert(0, str(REPO / "particle-life-app_gb300"))
+sys.path.insert(0, str(REPO / "oracle"))
+
+METRIC = "particle-steps/s at 1M 2D"
+UNIT = "particle-steps/s"
+FRICTION = 0.5 ** (1.0 / (60.0 * 0.043))
+
+# Algorithmic work per unit (FMA = 2 flops; compare and rsqrt = 1).
+FLOPS_PER_CANDIDATE = {2: 6, 3: 9}
+FLOPS_PER_INTERACTION = {2: 13, 3: 15}
+# Bytes each kernel must move per particle / per cell, by design (2D layout).
+BYTES = {"scatter": 12, "gather": 56, "force": 56, "scan_cell": 16}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=1_000_000)
+    ap.add_argument("--e2e-steps", type=int, default=30)
+    ap.add_argument("--cpu-sample-s", type=float, default=10.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-flush", action="store_true", help="keep L2 warm between steps (not a headline number)")
+    return ap.parse_args()
+
+
+def make_world(n: int, seed: int = 2024):
+    rng = np.random.Generator(np.random.Philox(seed))
+    pos = np.zeros((n, 3))
+    pos[:, :2] = rng.random((n, 2), dtype=np.float32)
+    vel = np.zeros((n, 3))
+    types = rng.integers(0, 8, n).astype(np.int32)
+    m = np.asarray(2 * rng.random((8, 8)) - 1, np.float32).astype(np.float64)
+    return pos, vel, types, m
+
+
+SETTINGS = dict(rmax=0.0025, friction=FRICTION, force=1.0, dt=0.01, beta=0.3, wrap=True)
+
+
+class Clocks:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "50"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except FileNotFoundError:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        self.proc.wait()
+        rows = [r.split(",") for r in Path(self.path).read_text().strip().splitlines() if r.strip()]
+        os.unlink(self.path)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            r = [x.strip() for x in r]
+            if len(r) < 9:
+                continue
+            try:
+                sm.append(float(r[1]))
+                smax.append(float(r[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, r[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_oracle_rate(n, threads, budget_s, steps_cap=None):
+    """Times the oracle (C FP64 restatement) on the workload: particle-steps/s."""
+    import orc
+
+    orc.build()
+    pos, vel, types, m = make_world(n)
+    w = orc.World(2, pos, vel, types, np.arange(n, dtype=np.int32), m,
+                  orc.settings(SETTINGS["rmax"], SETTINGS["friction"], SETTINGS["force"], SETTINGS["dt"],
+                               SETTINGS["beta"], SETTINGS["wrap"]))
+    t1 = w.run(1, threads)  # warm-up and estimate
+    steps = max(1, int(budget_s / max(t1, 1e-6)))
+    if steps_cap:
+        steps = min(steps, steps_cap)
+    t = w.run(steps, threads)
+    return n * steps / t, steps, t
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    import orc
+
+    orc.build()
+    n = args.n
+    pos, vel, types, m = make_world(n)
+    w = orc.World(2, pos, vel, types, np.arange(n, dtype=np.int32), m,
+                  orc.settings(SETTINGS["rmax"], SETTINGS["friction"], SETTINGS["force"], SETTINGS["dt"],
+                               SETTINGS["beta"], SETTINGS["wrap"]))
+    w.run(args.warmup, threads)
+    t = w.run(args.steps, threads)
+    v = n * args.steps / t
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Philox: uniform positions, zero velocity)",
+        "config": {"workload": f"2D periodic, N={n}, 8 types, rmax=0.0025 (unit box), dt=0.01, C FP64 "
+                               f"restatement of Physics.update() on {threads} host threads"},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{args.steps} full steps after {args.warmup} warm-up steps (Java/JDK absent: "
+                                   "C restatement of the reference's step, same algorithm and threading)"},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def run_ours(args):
+    import torch
+
+    import plgpu
+    from plgpu import _lib
+    from plgpu.physics import GpuWorld
+
+    rank = int(os.environ.get("RANK", "0"))
+    world_size = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world_size > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local_rank)
+        dist.init_process_group("nccl")
+    else:
+        torch.cuda.set_device(0)
+    dev = torch.device("cuda", torch.cuda.current_device())
+
+    import __graft_entry__
+
+    __graft_entry__.build()
+    lib = _lib.load()
+
+    n = args.n
+    pos, vel, types, m = make_world(n, seed=2024 + rank)
+    w = GpuWorld(2, n)
+    w.set_settings(**SETTINGS)
+    w.set_matrix(m)
+    w.upload(pos, vel, types)
+    stream = torch.cuda.ExternalStream(w.stream(), device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    def flush_l2():
+        if not args.no_flush:
+            flush.zero_()
+        torch.cuda.synchronize()
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    check = plgpu.physics.check
+    w.step(args.warmup)
+    clocks = Clocks(torch.cuda.current_device())
+    clocks.start()
+
+    # value: device-resident, each step timed alone, L2 flushed in between
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    barrier()
+    for k in range(args.steps):
+        flush_l2()
+        ev[k][0].record(stream)
+        check(lib.plg_step_async(w.ctx, 1), w.ctx, "plg_step_async")
+        ev[k][1].record(stream)
+        check(lib.plg_sync(w.ctx, 60.0), w.ctx, "plg_sync")
+    barrier()
+    total_ms = sum(a.elapsed_time(b) for a, b in ev)
+    if dist is not None:
+        t = torch.tensor([total_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    ms_per_step = total_ms / args.steps
+    value = world_size * n * args.steps / (total_ms * 1e-3)
+
+    # per-kernel durations over a profiled pass of the same number of steps
+    check(lib.plg_profile_enable(w.ctx, 1), w.ctx, "plg_profile_enable")
+    for k in range(args.steps):
+        flush_l2()
+        check(lib.plg_step(w.ctx, 1), w.ctx, "plg_step")
+    kern = {}
+    for k, name in enumerate(_lib.KERNELS):
+        ms = _lib.C.c_double()
+        cnt = _lib.C.c_int64()
+        lib.plg_profile_read(w.ctx, k, _lib.C.byref(ms), _lib.C.byref(cnt))
+        kern[name] = {"avg_us": 1e3 * ms.value / max(cnt.value, 1), "launches": cnt.value}
+    check(lib.plg_profile_enable(w.ctx, 0), w.ctx, "plg_profile_enable")
+
+    # e2e through the public API with pinned host buffers
+    hp = torch.empty((n, 3), dtype=torch.float64, pin_memory=True).numpy()
+    hv = torch.empty((n, 3), dtype=torch.float64, pin_memory=True).numpy()
+    ht = torch.empty(n, dtype=torch.int32, pin_memory=True).numpy()
+    hi = torch.empty(n, dtype=torch.int32, pin_memory=True).numpy()
+    P, I = _lib.C.c_double, _lib.C.c_int32
+    check(lib.plg_download(w.ctx, _lib.ptr(hp, P), _lib.ptr(hv, P), _lib.ptr(ht, I), _lib.ptr(hi, I)), w.ctx, "dl")
+    e2e_s = 0.0
+    barrier()
+    for k in range(args.e2e_steps):
+        flush_l2()
+        t0 = time.perf_counter()
+        check(lib.plg_upload(w.ctx, n, _lib.ptr(hp, P), _lib.ptr(hv, P), _lib.ptr(ht, I)), w.ctx, "plg_upload")
+        check(lib.plg_step(w.ctx, 1), w.ctx, "plg_step")
+        check(lib.plg_download(w.ctx, _lib.ptr(hp, P), _lib.ptr(hv, P), _lib.ptr(ht, I), _lib.ptr(hi, I)), w.ctx,
+              "plg_download")
+        e2e_s += time.perf_counter() - t0
+    barrier()
+    clk = clocks.stop()
+    if dist is not None:
+        t = torch.tensor([e2e_s], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_value = world_size * n * args.e2e_steps / e2e_s
+
+    # pair statistics of the current state (one instrumented step)
+    dbg = w.debug_step()
+    cand = dbg["candidates"] / n
+    inter = float(dbg["pairs"].mean())
+    w.close()
+
+    peak = _lib.C.c_double()
+    check(lib.plg_probe_fp32_peak(_lib.C.byref(peak)), None, "plg_probe_fp32_peak")
+    peaks = {}
+    pk = REPO / "MEASURED_PEAKS.json"
+    if pk.exists():
+        peaks = json.loads(pk.read_text())
+    hbm = peaks.get("hbm_gbs")
+
+    force_us = kern["force"]["avg_us"]
+    flops = n * (cand * FLOPS_PER_CANDIDATE[2] + inter * FLOPS_PER_INTERACTION[2])
+    achieved = flops / (force_us * 1e-6) / 1e12
+    traffic = None
+    tf = REPO / "profiles" / "force_2d_1m_traffic.json"
+    if tf.exists():
+        traffic = json.loads(tf.read_text()).get("dram_bytes_per_launch")
+    roofline = {"bound": "fp32", "kernel": "force", "achieved": achieved, "peak": peak.value, "unit": "TFLOP/s",
+                "frac": achieved / peak.value, "traffic": traffic,
+                "peak_source": "FFMA microbenchmark run live by this bench (MEASURED_PEAKS.json has no FP32 peak)",
+                "work": f"{cand:.2f} candidate + {inter:.2f} interacting pairs per particle; "
+                        f"{FLOPS_PER_CANDIDATE[2]} / {FLOPS_PER_INTERACTION[2]} flops each"}
+    sort_kernels = {}
+    if hbm:
+        cells = (int(np.floor(1 / SETTINGS["rmax"]))) ** 2
+        for name, b in (("scatter", BYTES["scatter"] * n), ("gather", BYTES["gather"] * n),
+                        ("scan_down", BYTES["scan_cell"] * cells), ("force", BYTES["force"] * n)):
+            gbs = b / (kern[name]["avg_us"] * 1e-6) / 1e9
+            sort_kernels[name] = {"achieved_gbs": gbs, "frac_of_measured_hbm": gbs / hbm}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        rate, steps, secs = cpu_oracle_rate(n, threads, args.cpu_sample_s)
+        cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"{steps} steps of the same 1M workload in {secs:.1f} s (C FP64 restatement of "
+                         f"Physics.update(), {threads} threads; no JDK for the Java path)"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world_size, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded Philox: uniform positions, zero velocity, uniform types and matrix)",
+            "config": {"workload": f"2D periodic unit box, N={n}, 8 types, rmax=0.0025 (0.005 in [-1,1]^2), "
+                                   "beta=0.3, friction t1/2=0.043 s, dt=0.01",
+                       "parallelism": "replicas" if world_size > 1 else "single GPU",
+                       "l2": "warm (not flushed)" if args.no_flush else "flushed (256 MB write) between steps"},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": n * (24 + 24 + 4),
+                    "d2h_bytes_per_step": n * (24 + 24 + 4 + 4), "steps": args.e2e_steps,
+                    "api": "plg_upload + plg_step + plg_download, pinned host buffers, host wall clock"},
+            "gpu_launches": 6 * args.steps,
+            "roofline": roofline,
+            "kernels": kern,
+            "sort_kernels_hbm": sort_kernels,
+            "pair_interactions_per_s": value * inter,
+            "candidates_per_particle": cand,
+            "interactions_per_particle": inter,
+            "cpu_baseline": cpu,
+            "clocks": clk,
+        }
+        print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,200 @@
+/*
+ * plgpu.h — C ABI of the GB300-native Particle Life physics step.
+ *
+ * One context (plg_ctx) holds one world: its particles in FP32 structure-of-
+ * arrays form in device memory, its PhysicsSettings mirror and its type
+ * matrix.  plg_step() advances the world exactly like
+ * com.particle_life.backend.Physics.update() does on the CPU:
+ *
+ *   makeContainers  (Physics.java:309-354)  -> device stable counting sort
+ *   updateVelocity  (Physics.java:397-441)  -> fused force kernel
+ *   Accelerator     (app/Main.java:275-280) -> fused into the force kernel
+ *   updatePosition  (Physics.java:443-450)  -> force kernel epilogue
+ *
+ * Reference paths are relative to src/main/java/com/particle_life/ of
+ * tom-mohr/particle-life-app.
+ *
+ * Conventions
+ *   - Every function returns a plg_status (0 = PLG_OK).  Nothing throws or
+ *     aborts across this boundary.  plg_last_error() gives a message.
+ *   - Host buffers are owned by the caller and are never retained after a
+ *     call returns.  The library owns all device memory.
+ *   - One context is driven by one thread at a time.  plg_request_stop() is
+ *     the only call that may come from another thread.
+ *   - Positions live in the reference's unit box [0,1)^d (wrap) or [0,1]^d
+ *     (clamp).  Host arrays use the PhysicsSnapshot layout
+ *     (app/PhysicsSnapshot.java:36-62): double[3n] interleaved x,y,z for
+ *     positions and velocities (z = 0 in 2D), int32[n] types.
+ *   - Particle ids are the upload index.  Like Physics.particles, the
+ *     particle order is permuted by every step (cell-sorted order); ids let a
+ *     caller map particles back.
+ */
+#ifndef PLGPU_H
+#define PLGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PLG_ABI_VERSION 1
+
+typedef enum plg_status {
+    PLG_OK = 0,
+    PLG_E_INVALID_ARG = 1, /* bad pointer, size, range or setting           */
+    PLG_E_UNSUPPORTED = 2, /* e.g. an accelerator other than particle-life  */
+    PLG_E_STATE = 3,       /* call order: step before settings/matrix/upload */
+    PLG_E_NO_MEMORY = 4,   /* device or pinned allocation failed            */
+    PLG_E_CUDA = 5,        /* a CUDA runtime call failed (no device, ...)   */
+    PLG_E_TIMEOUT = 6,     /* a bounded device wait ran out                 */
+    PLG_E_STOPPED = 7,     /* plg_request_stop() ended a multi-step call    */
+    PLG_E_DEVICE = 8,      /* a kernel raised its error word                */
+    PLG_E_CAPACITY = 9     /* more particles than the context was built for */
+} plg_status;
+
+/* The only accelerator with a device implementation: the default lambda of
+ * app/Main.java:275-280 with its beta (hard-coded 0.3 there) as a parameter.
+ * Any other kind is rejected with PLG_E_UNSUPPORTED: there is no CPU
+ * fallback.  Mirrors the Accelerator plug-in (backend/Accelerator.java:16). */
+#define PLG_ACCEL_PARTICLE_LIFE 1
+
+/* Mirror of backend/PhysicsSettings.java:8-38 (matrix passed separately). */
+typedef struct plg_settings {
+    double rmax;       /* interaction radius, also the cell size (0 < rmax <= 1) */
+    double friction;   /* per-1/60 s velocity factor, applied as pow(friction, 60 dt) */
+    double force;      /* force multiplier                                   */
+    double dt;         /* time step in seconds                               */
+    double beta;       /* accelerator parameter, 0 < beta < 1                */
+    int32_t wrap;      /* 1: periodic box (Range.wrap), 0: clamp (Range.clamp) */
+    int32_t accel_kind;/* PLG_ACCEL_PARTICLE_LIFE                            */
+} plg_settings;
+
+typedef struct plg_ctx plg_ctx;
+
+/* ---- library --------------------------------------------------------- */
+
+/* Version string of this build.  Host only. */
+const char* plg_version(void);
+
+/* Static description of a status code.  Host only. */
+const char* plg_status_string(int status);
+
+/* Checks a settings struct without touching a device.  Host only.
+ * Replaces nothing in the reference (Java accepts any doubles); it states
+ * the ranges the device path supports. */
+int plg_validate_settings(int dim, const plg_settings* s);
+
+/* The exact cell lookup table used on the device.  Host only.
+ * For cell size cs = rmax, nx = floor(1/cs) (Physics.java:82-85) and
+ * bounds[k] (k = 0..nx) = the smallest float x with (int)((double)x/cs) >= k,
+ * so that the reference's getContainerIndex (Physics.java:362-375) of an
+ * FP32 position equals the number of k >= 1 with x >= bounds[k], clamped to
+ * nx-1.  Writes *nx_out; writes bounds when bounds != NULL and cap > nx. */
+int plg_cell_bounds(double rmax, int32_t* nx_out, float* bounds, int64_t cap);
+
+/* ---- context ---------------------------------------------------------- */
+
+/* Creates a world of dimension 2 or 3 able to hold `capacity` particles on
+ * the current CUDA device.  Replaces the Physics constructor
+ * (Physics.java:65-80) minus the host-side setters, which stay in Java. */
+int plg_create(int dim, int64_t capacity, plg_ctx** out);
+
+int plg_destroy(plg_ctx* ctx);
+
+/* Settings: Physics.settings (Physics.java:13, PhysicsSettings.java:8-38).
+ * A change of rmax re-bins the particles before the next step. */
+int plg_set_settings(plg_ctx* ctx, const plg_settings* s);
+int plg_get_settings(plg_ctx* ctx, plg_settings* out);
+
+/* Type matrix: settings.matrix (Matrix.java:3-8, DefaultMatrix.java).
+ * `m` is row-major n x n doubles, m[i*n+j] = matrix.get(i, j); 1 <= n <= 1024. */
+int plg_set_matrix(plg_ctx* ctx, int32_t n, const double* m);
+
+/* Replaces the whole particle state: Physics.particles (Physics.java:15).
+ * pos, vel: double[3n] interleaved (z ignored in 2D); type: int32[n] with
+ * 0 <= type < matrix size; positions must lie in [0,1] per axis and be
+ * finite (use ensurePosition, Physics.java:499-505, before uploading).
+ * vel may be NULL (zero velocities).  Ids are assigned 0..n-1. */
+int plg_upload(plg_ctx* ctx, int64_t n, const double* pos, const double* vel,
+               const int32_t* type);
+
+/* nsteps x Physics.update() (Physics.java:112-134).  Blocks until done.
+ * Checks the stop flag between steps: a set flag ends the call early with
+ * PLG_E_STOPPED and is cleared (Physics.forceUpdateStop, Physics.java:149). */
+int plg_step(plg_ctx* ctx, int32_t nsteps);
+
+/* Enqueues nsteps without waiting; pair with plg_sync. */
+int plg_step_async(plg_ctx* ctx, int32_t nsteps);
+
+/* Waits for all enqueued work, polling at most timeout_s seconds
+ * (<= 0: no limit), and reports kernel error words.  PLG_E_TIMEOUT when the
+ * wait runs out; the context stays usable. */
+int plg_sync(plg_ctx* ctx, double timeout_s);
+
+/* Copies the current state to host buffers in the current (cell-sorted)
+ * order: the layout of PhysicsSnapshot.write (app/PhysicsSnapshot.java:36-62)
+ * plus the particle ids.  Any pointer may be NULL to skip that array. */
+int plg_download(plg_ctx* ctx, double* pos, double* vel, int32_t* type,
+                 int32_t* id);
+
+int plg_particle_count(plg_ctx* ctx, int64_t* n);
+
+/* Thread-safe stop request: Physics.forceUpdateStop (Physics.java:149-151)
+ * and Physics.kill (Physics.java:156-158).  Takes effect between steps. */
+int plg_request_stop(plg_ctx* ctx);
+
+/* Message of the last failing call on this context ("" if none). */
+const char* plg_last_error(plg_ctx* ctx);
+
+/* The cudaStream_t every kernel of this context is launched on, so a caller
+ * can order its own work and record CUDA events against it. */
+int plg_get_stream(plg_ctx* ctx, void** stream);
+
+/* 1 (default): each step is one CUDA graph launch.  0: plain launches. */
+int plg_set_use_graph(plg_ctx* ctx, int32_t on);
+
+/* ---- measurement ------------------------------------------------------ */
+
+/* Kernel ids for plg_profile_read. */
+#define PLG_K_SCAN_REDUCE 0
+#define PLG_K_SCAN_PARTS 1
+#define PLG_K_SCAN_DOWN 2
+#define PLG_K_SCATTER 3
+#define PLG_K_GATHER 4
+#define PLG_K_FORCE 5
+#define PLG_K_COUNT 6
+
+/* When on, steps run as plain launches bracketed by CUDA events on the
+ * context's stream; plg_profile_read returns per-kernel totals since the
+ * last enable.  Turning it on clears the totals. */
+int plg_profile_enable(plg_ctx* ctx, int32_t on);
+int plg_profile_read(plg_ctx* ctx, int32_t kernel, double* total_ms,
+                     int64_t* launches);
+const char* plg_kernel_name(int32_t kernel);
+
+/* Runs one step like plg_step with the instrumented force kernel and copies,
+ * per particle of the step's cell-sorted order (the order plg_download
+ * returns after it):
+ *   cell      int32[n]   getContainerIndex of the pre-step position
+ *   pairs     int32[n]   interacting pairs (d2 != 0 && d2 <= rmax^2)
+ *   hash_sum  uint64[n]  sum of mix64(id_j) over those pairs
+ *   hash_xor  uint64[n]  xor of mix64(id_j)
+ *   acc       float[dim*n] sum of Accelerator.accelerate(a, r/rmax) before
+ *                        the rmax*force*dt scale (Physics.java:435-437)
+ * and, in *candidates, the number of pairs tested.  Any pointer may be NULL.
+ * mix64 is the splitmix64 finaliser of the id. */
+int plg_debug_step(plg_ctx* ctx, int32_t* cell, int32_t* pairs,
+                   uint64_t* hash_sum, uint64_t* hash_xor, float* acc,
+                   int64_t* candidates);
+
+/* Device FP32 FMA throughput microbenchmark on the current device, in
+ * TFLOP/s (an FFMA counts 2 flops).  Runs for about 0.1 s. */
+int plg_probe_fp32_peak(double* tflops);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PLGPU_H */

@@ -1,0 +1,169 @@
+// plg_internal.cuh — device-side types and helpers shared by the kernels of
+// the Particle Life physics step (binning, force/integration, conversion).
+//
+// Data layout in HBM, one world, FP32 structure of arrays:
+//   2D: pt  float4 {x, y, type bits, id bits}   vel float2 {vx, vy}
+//   3D: pt  float4 {x, y, z, type bits}         vel float4 {vx, vy, vz, id bits}
+// Two copies (A = current order, B = cell-sorted order) alternate inside a
+// step: the sort gathers A into B, the force kernel reads B and writes the
+// next state into A, so positions that the velocity phase still reads are
+// never overwritten (the reason Physics.java:122-131 runs two phases).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace plg {
+
+constexpr unsigned kFull = 0xffffffffu;
+
+// Status bits raised by kernels into the context's device status word.
+enum DeviceStatus : uint32_t {
+    kDevBadPosition = 1u << 0,  // upload: position outside [0,1] or not finite
+    kDevBadType = 1u << 1,      // upload: type outside [0, matrix size)
+    kDevBadVelocity = 1u << 2,  // upload: velocity not finite
+    kDevSpinLimit = 1u << 3,    // a bounded device wait ran out
+};
+
+template <int D>
+struct Layout;
+
+template <>
+struct Layout<2> {
+    using Vel = float2;
+    static __device__ __forceinline__ int type(const float4& p) { return __float_as_int(p.z); }
+    static __device__ __forceinline__ int id(const float4& p, const Vel&) { return __float_as_int(p.w); }
+};
+
+template <>
+struct Layout<3> {
+    using Vel = float4;
+    static __device__ __forceinline__ int type(const float4& p) { return __float_as_int(p.w); }
+    static __device__ __forceinline__ int id(const float4&, const Vel& v) { return __float_as_int(v.w); }
+};
+
+// Uniform grid of the reference: cell size cs = rmax, nx = floor(1/cs) cells
+// per axis (Physics.java:82-85, 312-313).  `bounds` is the exact lookup table
+// built on the host: bounds[k] = smallest float x with (int)((double)x/cs) >= k.
+struct Grid {
+    int nx;
+    int ncells;           // nx^D
+    float inv_cs;         // (float)(1/cs): first guess only
+    float b_nx;           // bounds[nx]: x >= b_nx means (int)(x/cs) == nx
+    const float* bounds;  // nx + 1 entries
+};
+
+// (int)((double)x / cs) for an FP32 x in [0,1], bit-exact with the
+// reference's FP64 expression (Physics.java:363-364, 404-405): a float guess,
+// corrected by one table compare each way.  The guess is off by at most one
+// for nx < 2^21 (relative error <= 2^-23 of a quotient <= nx + 1).
+__device__ __forceinline__ int axis_cell_unclamped(float x, const Grid& g) {
+    int c = (int)(x * g.inv_cs);
+    c = min(max(c, 0), g.nx);
+    if (c > 0 && x < __ldg(g.bounds + c)) {
+        --c;
+    } else if (c < g.nx && x >= __ldg(g.bounds + c + 1)) {
+        ++c;
+    }
+    return c;
+}
+
+// getContainerIndex per axis: clamp cx == nx to nx - 1 (Physics.java:367-372).
+__device__ __forceinline__ int axis_cell(float x, const Grid& g) {
+    return min(axis_cell_unclamped(x, g), g.nx - 1);
+}
+
+template <int D>
+__device__ __forceinline__ uint32_t cell_index(float x, float y, float z, const Grid& g) {
+    uint32_t c = (uint32_t)axis_cell(x, g) + (uint32_t)axis_cell(y, g) * (uint32_t)g.nx;
+    if (D == 3) c += (uint32_t)axis_cell(z, g) * (uint32_t)g.nx * (uint32_t)g.nx;
+    return c;
+}
+
+// Counting step of makeContainers (Physics.java:328-332) for one particle per
+// lane: lanes of a warp with the same cell add once, and each lane's rank in
+// its cell follows lane order.  `mask` = lanes taking part (all must call).
+__device__ __forceinline__ uint32_t bin_count(uint32_t* counts, uint32_t cell, unsigned mask) {
+    const unsigned peers = __match_any_sync(mask, cell);
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(peers) - 1;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(counts + cell, (uint32_t)__popc(peers));
+    base = __shfl_sync(peers, base, leader);
+    return base + (uint32_t)__popc(peers & ((1u << lane) - 1u));
+}
+
+// splitmix64 output function (Steele, Lea, Flood 2014) on id + gamma: the
+// order-free pair hash of the parity checks.
+__host__ __device__ __forceinline__ uint64_t mix64(uint64_t id) {
+    uint64_t z = id + 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+// Parameters of the force / integration kernel, passed by value.
+struct ForceParams {
+    Grid g;
+    int n;
+    int wrap;
+    int ntypes;
+    int slmask_ok;          // nx >= 4: sliver targets need the stencil correction
+    const float* matrix;    // ntypes x ntypes, row-major, FP32
+    float lo, hi, tiny;     // FP32 d2 decision band around rmax^2
+    float inv_rmax;
+    float beta, inv_beta, one_plus_beta, inv_one_minus_beta;
+    float ff;               // (float) pow(friction, 60 dt)
+    float scale;            // (float) (rmax * force * dt)
+    float dt;
+    double rmax, rmax2, beta_d;
+};
+
+// Per-particle debug outputs of the instrumented force kernel.
+struct DebugOut {
+    int32_t* pairs;
+    unsigned long long* hsum;
+    unsigned long long* hxor;
+    float* acc;
+    unsigned long long* candidates;
+};
+
+template <int D>
+struct StateBuf {
+    float4* pt;
+    typename Layout<D>::Vel* vel;
+};
+
+// ---- launchers (defined in the .cu files, called by the host library) ----
+
+template <int D>
+void launch_upload(cudaStream_t st, int n, const double* pos, const double* vel, const int32_t* type,
+                   int ntypes, StateBuf<D> a, uint32_t* cell, uint32_t* rank, uint32_t* counts, Grid g,
+                   uint32_t* status);
+
+template <int D>
+void launch_rebin(cudaStream_t st, int n, StateBuf<D> a, uint32_t* cell, uint32_t* rank, uint32_t* counts,
+                  Grid g);
+
+template <int D>
+void launch_download(cudaStream_t st, int n, StateBuf<D> a, double* pos, double* vel, int32_t* type,
+                     int32_t* id);
+
+int scan_blocks(int ncells);
+void launch_scan_reduce(cudaStream_t st, const uint32_t* counts, int ncells, uint32_t* parts);
+void launch_scan_parts(cudaStream_t st, uint32_t* parts, int nparts);
+void launch_scan_down(cudaStream_t st, uint32_t* counts, int ncells, const uint32_t* parts, uint32_t* cstart);
+void launch_scatter(cudaStream_t st, int n, const uint32_t* cell, const uint32_t* rank, const uint32_t* cstart,
+                    uint32_t* perm);
+
+template <int D>
+void launch_gather(cudaStream_t st, int n, const uint32_t* perm, const uint32_t* cell, const uint32_t* cstart,
+                   StateBuf<D> a, StateBuf<D> b, int32_t* cell_sorted);
+
+template <int D>
+void launch_force(cudaStream_t st, const ForceParams& p, bool general, StateBuf<D> b, const uint32_t* cstart,
+                  StateBuf<D> a, uint32_t* cell, uint32_t* rank, uint32_t* counts, const DebugOut* dbg);
+
+cudaError_t probe_fp32_peak(double* tflops);
+
+}  // namespace plg

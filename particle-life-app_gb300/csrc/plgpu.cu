@@ -1,0 +1,775 @@
+// plgpu.cu — host side of the C ABI declared in include/plgpu.h.
+//
+// Owns one world per context: device buffers, the exact cell table, the
+// force-kernel parameters derived from PhysicsSettings, and a CUDA graph of
+// one step.  See plg_internal.cuh for the device data layout.
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <chrono>
+#include <climits>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "plg_internal.cuh"
+#include "plgpu.h"
+
+using namespace plg;
+
+namespace {
+
+constexpr int kRing = 4;                        // steps in flight per plg_step call
+constexpr int64_t kMaxParticles = INT_MAX / 2;  // 32-bit indices on the device
+constexpr int64_t kMaxCells = (int64_t)1 << 30;
+constexpr int kMaxAxisCells = 1 << 20;
+constexpr int kMaxTypes = 1024;
+constexpr double kBandRel = 1.0 / (1 << 19);  // FP32 decision band: 2^-19 relative
+
+const char* kKernelNames[PLG_K_COUNT] = {"scan_reduce", "scan_parts", "scan_down", "scatter", "gather", "force"};
+
+// Staging layout for host <-> device copies: pos[3n] vel[3n] (double), type[n] id[n] (int32).
+size_t stage_bytes(int64_t cap) { return (size_t)cap * (3 * 8 + 3 * 8 + 4 + 4); }
+
+}  // namespace
+
+struct plg_ctx {
+    int dim = 2;
+    int64_t cap = 0;
+    int64_t n = 0;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+
+    plg_settings s{};
+    bool have_settings = false;
+    bool have_matrix = false;
+    bool state_valid = false;  // an upload succeeded
+    bool bins_dirty = false;   // cell/rank/counts must be recomputed from A
+
+    // grid
+    int nx = 0;
+    int ncells = 0;
+    int nparts = 0;
+    std::vector<float> bounds_h;
+    float* bounds = nullptr;
+    int64_t bounds_cap = 0;
+    uint32_t* counts = nullptr;
+    uint32_t* cstart = nullptr;
+    int64_t cells_cap = 0;
+    int64_t cstart_cap = 0;
+    uint32_t* parts = nullptr;
+    int64_t parts_cap = 0;
+
+    // matrix
+    int ntypes = 0;
+    float* matrix = nullptr;
+    int64_t matrix_cap = 0;
+
+    // particles (A = current order, B = cell-sorted)
+    float4* apt = nullptr;
+    float4* bpt = nullptr;
+    void* avel = nullptr;
+    void* bvel = nullptr;
+    uint32_t* cell = nullptr;
+    uint32_t* rank = nullptr;
+    uint32_t* perm = nullptr;
+    unsigned char* stage = nullptr;
+
+    uint32_t* status_d = nullptr;
+    uint32_t* status_h = nullptr;
+
+    // instrumented step
+    int32_t* dbg_pairs = nullptr;
+    unsigned long long* dbg_hsum = nullptr;
+    unsigned long long* dbg_hxor = nullptr;
+    unsigned long long* dbg_cand = nullptr;
+    float* dbg_acc = nullptr;
+    int32_t* dbg_cell = nullptr;
+
+    // graph of one step
+    bool use_graph = true;
+    cudaGraphExec_t gexec = nullptr;
+    bool graph_dirty = true;
+
+    // profiling
+    bool profiling = false;
+    cudaEvent_t pev[PLG_K_COUNT][2] = {};
+    double prof_ms[PLG_K_COUNT] = {};
+    int64_t prof_n[PLG_K_COUNT] = {};
+
+    cudaEvent_t ring[kRing] = {};
+    int ring_pos = 0;
+    int ring_fill = 0;
+
+    std::atomic<int> stop{0};
+    std::string err;
+    ForceParams fp{};
+    bool general = false;
+};
+
+namespace {
+
+int set_err(plg_ctx* c, int code, const std::string& msg) {
+    if (c) c->err = msg;
+    return code;
+}
+
+int cuda_fail(plg_ctx* c, const char* what, cudaError_t e) {
+    cudaGetLastError();  // clear a non-sticky error
+    return set_err(c, PLG_E_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define CK(ctx, call)                                          \
+    do {                                                       \
+        cudaError_t e_ = (call);                               \
+        if (e_ != cudaSuccess) return cuda_fail(ctx, #call, e_); \
+    } while (0)
+
+struct DeviceGuard {
+    int prev = -1;
+    explicit DeviceGuard(int d) {
+        if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+        if (prev != d) cudaSetDevice(d);
+    }
+    ~DeviceGuard() {
+        int cur = -1;
+        if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
+    }
+};
+
+template <typename T>
+int grow(plg_ctx* c, T** p, int64_t* cap, int64_t need, const char* what) {
+    if (*p && *cap >= need) return PLG_OK;
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+    *cap = 0;
+    cudaError_t e = cudaMalloc((void**)p, sizeof(T) * (size_t)(need > 0 ? need : 1));
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        *p = nullptr;
+        return set_err(c, PLG_E_NO_MEMORY, std::string("cudaMalloc ") + what + ": " + cudaGetErrorString(e));
+    }
+    *cap = need;
+    return PLG_OK;
+}
+
+// bounds[k] = smallest float x >= 0 with (double)x / cs >= k (k = 1..nx);
+// bounds[0] = 0.  (int)((double)x/cs) >= k  <=>  (double)x/cs >= k.
+void build_bounds(double cs, int nx, float* b) {
+    b[0] = 0.f;
+    for (int k = 1; k <= nx; ++k) {
+        float f = (float)(k * cs);
+        while (!((double)f / cs >= (double)k)) f = std::nextafter(f, INFINITY);
+        for (;;) {
+            const float g = std::nextafter(f, -INFINITY);
+            if (g < 0.f || !((double)g / cs >= (double)k)) break;
+            f = g;
+        }
+        b[k] = f;
+    }
+}
+
+int grid_n(double rmax) { return (int)std::floor(1 / rmax); }
+
+void destroy_graph(plg_ctx* c) {
+    if (c->gexec) cudaGraphExecDestroy(c->gexec);
+    c->gexec = nullptr;
+    c->graph_dirty = true;
+}
+
+template <int D>
+StateBuf<D> buf_a(plg_ctx* c) {
+    return StateBuf<D>{c->apt, (typename Layout<D>::Vel*)c->avel};
+}
+template <int D>
+StateBuf<D> buf_b(plg_ctx* c) {
+    return StateBuf<D>{c->bpt, (typename Layout<D>::Vel*)c->bvel};
+}
+
+void compute_force_params(plg_ctx* c) {
+    const plg_settings& s = c->s;
+    ForceParams& p = c->fp;
+    p.g.nx = c->nx;
+    p.g.ncells = c->ncells;
+    p.g.inv_cs = (float)(1.0 / s.rmax);
+    p.g.b_nx = c->bounds_h[c->nx];
+    p.g.bounds = c->bounds;
+    p.n = (int)c->n;
+    p.wrap = s.wrap ? 1 : 0;
+    p.ntypes = c->ntypes;
+    p.slmask_ok = c->nx >= 4 ? 1 : 0;
+    p.matrix = c->matrix;
+    const double r2 = s.rmax * s.rmax;
+    const double lo_d = r2 * (1.0 - kBandRel), hi_d = r2 * (1.0 + kBandRel);
+    float lo = (float)lo_d, hi = (float)hi_d;
+    if ((double)lo > lo_d) lo = std::nextafter(lo, 0.f);
+    if ((double)hi < hi_d) hi = std::nextafter(hi, INFINITY);
+    p.lo = lo;
+    p.hi = hi;
+    p.tiny = std::ldexp(1.0f, -100);
+    p.inv_rmax = (float)(1.0 / s.rmax);
+    p.beta = (float)s.beta;
+    p.inv_beta = (float)(1.0 / s.beta);
+    p.one_plus_beta = (float)(1.0 + s.beta);
+    p.inv_one_minus_beta = (float)(1.0 / (1.0 - s.beta));
+    p.ff = (float)std::pow(s.friction, 60 * s.dt);
+    p.scale = (float)(s.rmax * s.force * s.dt);
+    p.dt = (float)s.dt;
+    p.rmax = s.rmax;
+    p.rmax2 = r2;
+    p.beta_d = s.beta;
+    c->general = c->nx < 3;
+}
+
+Grid grid_of(plg_ctx* c) { return c->fp.g; }
+
+// Enqueues the body of one step (no rebin) on c->stream.
+template <int D>
+void enqueue_body(plg_ctx* c, const DebugOut* dbg, int32_t* cell_sorted) {
+    cudaStream_t st = c->stream;
+    const int n = (int)c->n;
+    auto k0 = [&](int k) {
+        if (c->profiling) cudaEventRecord(c->pev[k][0], st);
+    };
+    auto k1 = [&](int k) {
+        if (c->profiling) cudaEventRecord(c->pev[k][1], st);
+    };
+    k0(PLG_K_SCAN_REDUCE);
+    launch_scan_reduce(st, c->counts, c->ncells, c->parts);
+    k1(PLG_K_SCAN_REDUCE);
+    k0(PLG_K_SCAN_PARTS);
+    launch_scan_parts(st, c->parts, c->nparts);
+    k1(PLG_K_SCAN_PARTS);
+    k0(PLG_K_SCAN_DOWN);
+    launch_scan_down(st, c->counts, c->ncells, c->parts, c->cstart);
+    k1(PLG_K_SCAN_DOWN);
+    k0(PLG_K_SCATTER);
+    launch_scatter(st, n, c->cell, c->rank, c->cstart, c->perm);
+    k1(PLG_K_SCATTER);
+    k0(PLG_K_GATHER);
+    launch_gather<D>(st, n, c->perm, c->cell, c->cstart, buf_a<D>(c), buf_b<D>(c), cell_sorted);
+    k1(PLG_K_GATHER);
+    k0(PLG_K_FORCE);
+    launch_force<D>(st, c->fp, c->general, buf_b<D>(c), c->cstart, buf_a<D>(c), c->cell, c->rank, c->counts, dbg);
+    k1(PLG_K_FORCE);
+}
+
+void enqueue_body_dim(plg_ctx* c, const DebugOut* dbg, int32_t* cell_sorted) {
+    if (c->dim == 2)
+        enqueue_body<2>(c, dbg, cell_sorted);
+    else
+        enqueue_body<3>(c, dbg, cell_sorted);
+}
+
+int enqueue_rebin(plg_ctx* c) {
+    if (!c->bins_dirty) return PLG_OK;
+    CK(c, cudaMemsetAsync(c->counts, 0, sizeof(uint32_t) * (size_t)c->ncells, c->stream));
+    if (c->dim == 2)
+        launch_rebin<2>(c->stream, (int)c->n, buf_a<2>(c), c->cell, c->rank, c->counts, grid_of(c));
+    else
+        launch_rebin<3>(c->stream, (int)c->n, buf_a<3>(c), c->cell, c->rank, c->counts, grid_of(c));
+    CK(c, cudaGetLastError());
+    c->bins_dirty = false;
+    return PLG_OK;
+}
+
+int accumulate_profile(plg_ctx* c) {
+    CK(c, cudaEventSynchronize(c->pev[PLG_K_FORCE][1]));
+    for (int k = 0; k < PLG_K_COUNT; ++k) {
+        float ms = 0.f;
+        CK(c, cudaEventElapsedTime(&ms, c->pev[k][0], c->pev[k][1]));
+        c->prof_ms[k] += ms;
+        c->prof_n[k] += 1;
+    }
+    return PLG_OK;
+}
+
+int enqueue_step(plg_ctx* c) {
+    int rc = enqueue_rebin(c);
+    if (rc) return rc;
+    if (c->profiling) {
+        enqueue_body_dim(c, nullptr, nullptr);
+        CK(c, cudaGetLastError());
+        return accumulate_profile(c);
+    }
+    if (!c->use_graph) {
+        enqueue_body_dim(c, nullptr, nullptr);
+        CK(c, cudaGetLastError());
+        return PLG_OK;
+    }
+    if (c->graph_dirty || !c->gexec) {
+        destroy_graph(c);
+        cudaGraph_t g = nullptr;
+        CK(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+        enqueue_body_dim(c, nullptr, nullptr);
+        cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+        if (e != cudaSuccess) return cuda_fail(c, "cudaStreamEndCapture", e);
+        e = cudaGraphInstantiate(&c->gexec, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) {
+            c->gexec = nullptr;
+            return cuda_fail(c, "cudaGraphInstantiate", e);
+        }
+        c->graph_dirty = false;
+    }
+    CK(c, cudaGraphLaunch(c->gexec, c->stream));
+    return PLG_OK;
+}
+
+int check_ready(plg_ctx* c) {
+    if (!c) return PLG_E_INVALID_ARG;
+    if (!c->have_settings) return set_err(c, PLG_E_STATE, "plg_set_settings has not been called");
+    if (!c->have_matrix) return set_err(c, PLG_E_STATE, "plg_set_matrix has not been called");
+    if (!c->state_valid) return set_err(c, PLG_E_STATE, "no valid particle state: call plg_upload");
+    return PLG_OK;
+}
+
+int wait_stream(plg_ctx* c, double timeout_s) {
+    if (timeout_s <= 0) {
+        CK(c, cudaStreamSynchronize(c->stream));
+    } else {
+        const auto t0 = std::chrono::steady_clock::now();
+        for (;;) {
+            cudaError_t e = cudaStreamQuery(c->stream);
+            if (e == cudaSuccess) break;
+            if (e != cudaErrorNotReady) return cuda_fail(c, "cudaStreamQuery", e);
+            const double el = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+            if (el > timeout_s) return set_err(c, PLG_E_TIMEOUT, "device work did not finish within the timeout");
+            std::this_thread::sleep_for(std::chrono::microseconds(50));
+        }
+    }
+    c->ring_fill = 0;
+    return PLG_OK;
+}
+
+int read_status(plg_ctx* c) {
+    CK(c, cudaMemcpyAsync(c->status_h, c->status_d, sizeof(uint32_t), cudaMemcpyDeviceToHost, c->stream));
+    CK(c, cudaStreamSynchronize(c->stream));
+    const uint32_t st = *c->status_h;
+    if (st == 0) return PLG_OK;
+    std::string m = "device reported:";
+    if (st & kDevBadPosition) m += " position outside [0,1] or not finite;";
+    if (st & kDevBadType) m += " type outside [0, matrix size);";
+    if (st & kDevBadVelocity) m += " velocity not finite;";
+    if (st & kDevSpinLimit) m += " bounded wait ran out;";
+    CK(c, cudaMemsetAsync(c->status_d, 0, sizeof(uint32_t), c->stream));
+    return set_err(c, (st & (kDevBadPosition | kDevBadType | kDevBadVelocity)) ? PLG_E_INVALID_ARG : PLG_E_DEVICE, m);
+}
+
+int free_all(plg_ctx* c) {
+    destroy_graph(c);
+    void* ptrs[] = {c->bounds, c->counts, c->cstart, c->parts, c->matrix, c->apt, c->bpt, c->avel, c->bvel,
+                    c->cell, c->rank, c->perm, c->stage, c->status_d, c->dbg_pairs, c->dbg_hsum, c->dbg_hxor,
+                    c->dbg_cand, c->dbg_acc, c->dbg_cell};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    if (c->status_h) cudaFreeHost(c->status_h);
+    for (int k = 0; k < PLG_K_COUNT; ++k)
+        for (int j = 0; j < 2; ++j)
+            if (c->pev[k][j]) cudaEventDestroy(c->pev[k][j]);
+    for (int k = 0; k < kRing; ++k)
+        if (c->ring[k]) cudaEventDestroy(c->ring[k]);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    return PLG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* plg_version(void) { return "plgpu 0.1.0 (sm_103a, ABI 1)"; }
+
+const char* plg_status_string(int status) {
+    switch (status) {
+        case PLG_OK: return "ok";
+        case PLG_E_INVALID_ARG: return "invalid argument";
+        case PLG_E_UNSUPPORTED: return "unsupported";
+        case PLG_E_STATE: return "invalid call order";
+        case PLG_E_NO_MEMORY: return "out of memory";
+        case PLG_E_CUDA: return "CUDA error";
+        case PLG_E_TIMEOUT: return "timeout";
+        case PLG_E_STOPPED: return "stopped";
+        case PLG_E_DEVICE: return "device error";
+        case PLG_E_CAPACITY: return "capacity exceeded";
+        default: return "unknown status";
+    }
+}
+
+int plg_validate_settings(int dim, const plg_settings* s) {
+    if (dim != 2 && dim != 3) return PLG_E_INVALID_ARG;
+    if (!s) return PLG_E_INVALID_ARG;
+    if (s->accel_kind != PLG_ACCEL_PARTICLE_LIFE) return PLG_E_UNSUPPORTED;
+    if (!(std::isfinite(s->rmax) && s->rmax > 0 && s->rmax <= 1)) return PLG_E_INVALID_ARG;
+    const int nx = grid_n(s->rmax);
+    if (nx < 1 || nx > kMaxAxisCells) return PLG_E_INVALID_ARG;
+    int64_t cells = (int64_t)nx * nx;
+    if (dim == 3) cells *= nx;
+    if (cells > kMaxCells) return PLG_E_INVALID_ARG;
+    if (!(std::isfinite(s->friction) && s->friction >= 0)) return PLG_E_INVALID_ARG;
+    if (!std::isfinite(s->force) || !std::isfinite(s->dt)) return PLG_E_INVALID_ARG;
+    if (!(std::isfinite(s->beta) && s->beta > 0 && s->beta < 1)) return PLG_E_INVALID_ARG;
+    if (s->wrap != 0 && s->wrap != 1) return PLG_E_INVALID_ARG;
+    return PLG_OK;
+}
+
+int plg_cell_bounds(double rmax, int32_t* nx_out, float* bounds, int64_t cap) {
+    if (!(std::isfinite(rmax) && rmax > 0 && rmax <= 1)) return PLG_E_INVALID_ARG;
+    const int nx = grid_n(rmax);
+    if (nx < 1 || nx > kMaxAxisCells) return PLG_E_INVALID_ARG;
+    if (nx_out) *nx_out = nx;
+    if (bounds) {
+        if (cap < (int64_t)nx + 1) return PLG_E_INVALID_ARG;
+        build_bounds(rmax, nx, bounds);
+    }
+    return PLG_OK;
+}
+
+int plg_create(int dim, int64_t capacity, plg_ctx** out) {
+    if (!out) return PLG_E_INVALID_ARG;
+    *out = nullptr;
+    if ((dim != 2 && dim != 3) || capacity < 1 || capacity > kMaxParticles) return PLG_E_INVALID_ARG;
+    plg_ctx* c = new (std::nothrow) plg_ctx();
+    if (!c) return PLG_E_NO_MEMORY;
+    c->dim = dim;
+    c->cap = capacity;
+    cudaError_t e = cudaGetDevice(&c->device);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        delete c;
+        return PLG_E_CUDA;
+    }
+    int rc = PLG_OK;
+    const size_t vel_sz = dim == 2 ? sizeof(float2) : sizeof(float4);
+    auto dmalloc = [&](void** p, size_t bytes) {
+        if (rc) return;
+        cudaError_t err = cudaMalloc(p, bytes);
+        if (err != cudaSuccess) {
+            cudaGetLastError();
+            *p = nullptr;
+            rc = err == cudaErrorMemoryAllocation ? PLG_E_NO_MEMORY : PLG_E_CUDA;
+        }
+    };
+    const size_t cap = (size_t)capacity;
+    e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) rc = PLG_E_CUDA;
+    dmalloc((void**)&c->apt, sizeof(float4) * cap);
+    dmalloc((void**)&c->bpt, sizeof(float4) * cap);
+    dmalloc(&c->avel, vel_sz * cap);
+    dmalloc(&c->bvel, vel_sz * cap);
+    dmalloc((void**)&c->cell, sizeof(uint32_t) * cap);
+    dmalloc((void**)&c->rank, sizeof(uint32_t) * cap);
+    dmalloc((void**)&c->perm, sizeof(uint32_t) * cap);
+    dmalloc((void**)&c->stage, stage_bytes(capacity));
+    dmalloc((void**)&c->status_d, 64);
+    if (!rc && cudaMallocHost((void**)&c->status_h, 64) != cudaSuccess) rc = PLG_E_NO_MEMORY;
+    for (int k = 0; k < kRing && !rc; ++k)
+        if (cudaEventCreateWithFlags(&c->ring[k], cudaEventDisableTiming) != cudaSuccess) rc = PLG_E_CUDA;
+    if (!rc && cudaMemset(c->status_d, 0, 64) != cudaSuccess) rc = PLG_E_CUDA;
+    if (rc) {
+        cudaGetLastError();
+        free_all(c);
+        delete c;
+        return rc;
+    }
+    *out = c;
+    return PLG_OK;
+}
+
+int plg_destroy(plg_ctx* c) {
+    if (!c) return PLG_E_INVALID_ARG;
+    {
+        DeviceGuard g(c->device);
+        if (c->stream) cudaStreamSynchronize(c->stream);
+        free_all(c);
+    }
+    delete c;
+    return PLG_OK;
+}
+
+int plg_set_settings(plg_ctx* c, const plg_settings* s) {
+    if (!c || !s) return PLG_E_INVALID_ARG;
+    int rc = plg_validate_settings(c->dim, s);
+    if (rc == PLG_E_UNSUPPORTED)
+        return set_err(c, rc, "only PLG_ACCEL_PARTICLE_LIFE has a device implementation (no CPU fallback)");
+    if (rc) return set_err(c, rc, "settings out of the supported range");
+    DeviceGuard g(c->device);
+    const bool grid_change = !c->have_settings || c->s.rmax != s->rmax;
+    if (grid_change) {
+        const int nx = grid_n(s->rmax);
+        int64_t cells = (int64_t)nx * nx * (c->dim == 3 ? nx : 1);
+        CK(c, cudaStreamSynchronize(c->stream));
+        if ((rc = grow(c, &c->bounds, &c->bounds_cap, (int64_t)nx + 1, "bounds"))) return rc;
+        if ((rc = grow(c, &c->counts, &c->cells_cap, cells, "counts"))) return rc;
+        if ((rc = grow(c, &c->cstart, &c->cstart_cap, cells + 1, "cstart"))) return rc;
+        const int nparts = scan_blocks((int)cells);
+        if ((rc = grow(c, &c->parts, &c->parts_cap, nparts, "parts"))) return rc;
+        c->nx = nx;
+        c->ncells = (int)cells;
+        c->nparts = nparts;
+        c->bounds_h.assign((size_t)nx + 1, 0.f);
+        build_bounds(s->rmax, nx, c->bounds_h.data());
+        CK(c, cudaMemcpy(c->bounds, c->bounds_h.data(), sizeof(float) * (size_t)(nx + 1), cudaMemcpyHostToDevice));
+        CK(c, cudaMemset(c->counts, 0, sizeof(uint32_t) * (size_t)cells));
+        if (c->state_valid) c->bins_dirty = true;
+    }
+    c->s = *s;
+    c->have_settings = true;
+    compute_force_params(c);
+    c->graph_dirty = true;
+    return PLG_OK;
+}
+
+int plg_get_settings(plg_ctx* c, plg_settings* out) {
+    if (!c || !out) return PLG_E_INVALID_ARG;
+    if (!c->have_settings) return set_err(c, PLG_E_STATE, "plg_set_settings has not been called");
+    *out = c->s;
+    return PLG_OK;
+}
+
+int plg_set_matrix(plg_ctx* c, int32_t n, const double* m) {
+    if (!c || !m || n < 1 || n > kMaxTypes) return set_err(c, PLG_E_INVALID_ARG, "matrix size must be 1..1024");
+    std::vector<float> f((size_t)n * n);
+    for (size_t k = 0; k < f.size(); ++k) {
+        if (!std::isfinite(m[k])) return set_err(c, PLG_E_INVALID_ARG, "matrix entries must be finite");
+        f[k] = (float)m[k];
+    }
+    DeviceGuard g(c->device);
+    int rc;
+    CK(c, cudaStreamSynchronize(c->stream));
+    if ((rc = grow(c, &c->matrix, &c->matrix_cap, (int64_t)n * n, "matrix"))) return rc;
+    CK(c, cudaMemcpy(c->matrix, f.data(), sizeof(float) * f.size(), cudaMemcpyHostToDevice));
+    if (c->ntypes != n || !c->have_matrix) c->graph_dirty = true;
+    if (c->have_matrix && n < c->ntypes && c->state_valid) {
+        // Types >= n would index outside the matrix: the caller must re-type
+        // first (Physics.setMatrixSize -> ensureTypes, Physics.java:238-272).
+        c->state_valid = false;
+        c->ntypes = n;
+        c->have_matrix = true;
+        if (c->have_settings) compute_force_params(c);
+        return set_err(c, PLG_E_STATE, "matrix shrank below the uploaded types: re-upload with ensured types");
+    }
+    c->ntypes = n;
+    c->have_matrix = true;
+    if (c->have_settings) compute_force_params(c);
+    c->graph_dirty = true;
+    return PLG_OK;
+}
+
+int plg_upload(plg_ctx* c, int64_t n, const double* pos, const double* vel, const int32_t* type) {
+    if (!c) return PLG_E_INVALID_ARG;
+    if (n < 0) return set_err(c, PLG_E_INVALID_ARG, "negative particle count");
+    if (n > c->cap) return set_err(c, PLG_E_CAPACITY, "more particles than the context capacity");
+    if (n > 0 && (!pos || !type)) return set_err(c, PLG_E_INVALID_ARG, "pos and type must not be NULL");
+    if (!c->have_settings) return set_err(c, PLG_E_STATE, "plg_set_settings has not been called");
+    if (!c->have_matrix) return set_err(c, PLG_E_STATE, "plg_set_matrix has not been called");
+    DeviceGuard g(c->device);
+    cudaStream_t st = c->stream;
+    double* dpos = (double*)c->stage;
+    double* dvel = dpos + 3 * (size_t)c->cap;
+    int32_t* dtype = (int32_t*)(dvel + 3 * (size_t)c->cap);
+    c->state_valid = false;
+    if (n > 0) {
+        CK(c, cudaMemcpyAsync(dpos, pos, sizeof(double) * 3 * (size_t)n, cudaMemcpyHostToDevice, st));
+        if (vel) CK(c, cudaMemcpyAsync(dvel, vel, sizeof(double) * 3 * (size_t)n, cudaMemcpyHostToDevice, st));
+        CK(c, cudaMemcpyAsync(dtype, type, sizeof(int32_t) * (size_t)n, cudaMemcpyHostToDevice, st));
+    }
+    CK(c, cudaMemsetAsync(c->counts, 0, sizeof(uint32_t) * (size_t)c->ncells, st));
+    CK(c, cudaMemsetAsync(c->status_d, 0, sizeof(uint32_t), st));
+    if (c->dim == 2)
+        launch_upload<2>(st, (int)n, dpos, vel ? dvel : nullptr, dtype, c->ntypes, buf_a<2>(c), c->cell, c->rank,
+                         c->counts, grid_of(c), c->status_d);
+    else
+        launch_upload<3>(st, (int)n, dpos, vel ? dvel : nullptr, dtype, c->ntypes, buf_a<3>(c), c->cell, c->rank,
+                         c->counts, grid_of(c), c->status_d);
+    CK(c, cudaGetLastError());
+    int rc = read_status(c);
+    if (rc) return rc;
+    if (c->n != n) c->graph_dirty = true;
+    c->n = n;
+    c->fp.n = (int)n;
+    c->bins_dirty = false;
+    c->state_valid = true;
+    return PLG_OK;
+}
+
+int plg_step_async(plg_ctx* c, int32_t nsteps) {
+    int rc = check_ready(c);
+    if (rc) return rc;
+    if (nsteps < 0) return set_err(c, PLG_E_INVALID_ARG, "negative step count");
+    DeviceGuard g(c->device);
+    for (int32_t k = 0; k < nsteps; ++k) {
+        if (c->stop.exchange(0)) return set_err(c, PLG_E_STOPPED, "stopped by plg_request_stop");
+        if (c->ring_fill == kRing) {
+            CK(c, cudaEventSynchronize(c->ring[c->ring_pos]));
+            c->ring_fill--;
+        }
+        if ((rc = enqueue_step(c))) return rc;
+        CK(c, cudaEventRecord(c->ring[c->ring_pos], c->stream));
+        c->ring_pos = (c->ring_pos + 1) % kRing;
+        c->ring_fill++;
+    }
+    return PLG_OK;
+}
+
+int plg_sync(plg_ctx* c, double timeout_s) {
+    if (!c) return PLG_E_INVALID_ARG;
+    DeviceGuard g(c->device);
+    int rc = wait_stream(c, timeout_s);
+    if (rc) return rc;
+    return read_status(c);
+}
+
+int plg_step(plg_ctx* c, int32_t nsteps) {
+    int rc = plg_step_async(c, nsteps);
+    if (rc == PLG_E_STOPPED) {
+        std::string m = c->err;
+        int r2 = plg_sync(c, 0);
+        if (r2) return r2;
+        c->err = m;
+        return rc;
+    }
+    if (rc) return rc;
+    return plg_sync(c, 0);
+}
+
+int plg_download(plg_ctx* c, double* pos, double* vel, int32_t* type, int32_t* id) {
+    if (!c) return PLG_E_INVALID_ARG;
+    if (!c->state_valid) return set_err(c, PLG_E_STATE, "no valid particle state: call plg_upload");
+    DeviceGuard g(c->device);
+    cudaStream_t st = c->stream;
+    const size_t n = (size_t)c->n;
+    double* dpos = (double*)c->stage;
+    double* dvel = dpos + 3 * (size_t)c->cap;
+    int32_t* dtype = (int32_t*)(dvel + 3 * (size_t)c->cap);
+    int32_t* did = dtype + (size_t)c->cap;
+    if (n > 0) {
+        if (c->dim == 2)
+            launch_download<2>(st, (int)n, buf_a<2>(c), pos ? dpos : nullptr, vel ? dvel : nullptr,
+                               type ? dtype : nullptr, id ? did : nullptr);
+        else
+            launch_download<3>(st, (int)n, buf_a<3>(c), pos ? dpos : nullptr, vel ? dvel : nullptr,
+                               type ? dtype : nullptr, id ? did : nullptr);
+        CK(c, cudaGetLastError());
+        if (pos) CK(c, cudaMemcpyAsync(pos, dpos, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, st));
+        if (vel) CK(c, cudaMemcpyAsync(vel, dvel, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, st));
+        if (type) CK(c, cudaMemcpyAsync(type, dtype, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, st));
+        if (id) CK(c, cudaMemcpyAsync(id, did, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, st));
+    }
+    CK(c, cudaStreamSynchronize(st));
+    return PLG_OK;
+}
+
+int plg_particle_count(plg_ctx* c, int64_t* n) {
+    if (!c || !n) return PLG_E_INVALID_ARG;
+    *n = c->n;
+    return PLG_OK;
+}
+
+int plg_request_stop(plg_ctx* c) {
+    if (!c) return PLG_E_INVALID_ARG;
+    c->stop.store(1);
+    return PLG_OK;
+}
+
+const char* plg_last_error(plg_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+int plg_get_stream(plg_ctx* c, void** stream) {
+    if (!c || !stream) return PLG_E_INVALID_ARG;
+    *stream = (void*)c->stream;
+    return PLG_OK;
+}
+
+int plg_set_use_graph(plg_ctx* c, int32_t on) {
+    if (!c) return PLG_E_INVALID_ARG;
+    c->use_graph = on != 0;
+    return PLG_OK;
+}
+
+int plg_profile_enable(plg_ctx* c, int32_t on) {
+    if (!c) return PLG_E_INVALID_ARG;
+    DeviceGuard g(c->device);
+    if (on) {
+        for (int k = 0; k < PLG_K_COUNT; ++k) {
+            for (int j = 0; j < 2; ++j)
+                if (!c->pev[k][j]) CK(c, cudaEventCreate(&c->pev[k][j]));
+            c->prof_ms[k] = 0;
+            c->prof_n[k] = 0;
+        }
+    }
+    c->profiling = on != 0;
+    return PLG_OK;
+}
+
+int plg_profile_read(plg_ctx* c, int32_t kernel, double* total_ms, int64_t* launches) {
+    if (!c || kernel < 0 || kernel >= PLG_K_COUNT) return PLG_E_INVALID_ARG;
+    if (total_ms) *total_ms = c->prof_ms[kernel];
+    if (launches) *launches = c->prof_n[kernel];
+    return PLG_OK;
+}
+
+const char* plg_kernel_name(int32_t kernel) {
+    if (kernel < 0 || kernel >= PLG_K_COUNT) return "";
+    return kKernelNames[kernel];
+}
+
+int plg_debug_step(plg_ctx* c, int32_t* cell, int32_t* pairs, uint64_t* hash_sum, uint64_t* hash_xor, float* acc,
+                   int64_t* candidates) {
+    int rc = check_ready(c);
+    if (rc) return rc;
+    DeviceGuard g(c->device);
+    const size_t cap = (size_t)c->cap;
+    auto dm = [&](void** p, size_t bytes) -> int {
+        if (*p) return PLG_OK;
+        cudaError_t e = cudaMalloc(p, bytes);
+        if (e != cudaSuccess) {
+            *p = nullptr;
+            return cuda_fail(c, "cudaMalloc (debug buffers)", e);
+        }
+        return PLG_OK;
+    };
+    if ((rc = dm((void**)&c->dbg_pairs, sizeof(int32_t) * cap))) return rc;
+    if ((rc = dm((void**)&c->dbg_hsum, sizeof(unsigned long long) * cap))) return rc;
+    if ((rc = dm((void**)&c->dbg_hxor, sizeof(unsigned long long) * cap))) return rc;
+    if ((rc = dm((void**)&c->dbg_cand, sizeof(unsigned long long)))) return rc;
+    if ((rc = dm((void**)&c->dbg_acc, sizeof(float) * 3 * cap))) return rc;
+    if ((rc = dm((void**)&c->dbg_cell, sizeof(int32_t) * cap))) return rc;
+    if ((rc = enqueue_rebin(c))) return rc;
+    CK(c, cudaMemsetAsync(c->dbg_cand, 0, sizeof(unsigned long long), c->stream));
+    DebugOut d{c->dbg_pairs, c->dbg_hsum, c->dbg_hxor, c->dbg_acc, c->dbg_cand};
+    const bool prof = c->profiling;
+    c->profiling = false;
+    enqueue_body_dim(c, &d, c->dbg_cell);
+    c->profiling = prof;
+    CK(c, cudaGetLastError());
+    const size_t n = (size_t)c->n;
+    cudaStream_t st = c->stream;
+    unsigned long long cand = 0;
+    if (n > 0) {
+        if (cell) CK(c, cudaMemcpyAsync(cell, c->dbg_cell, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, st));
+        if (pairs) CK(c, cudaMemcpyAsync(pairs, c->dbg_pairs, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, st));
+        if (hash_sum) CK(c, cudaMemcpyAsync(hash_sum, c->dbg_hsum, 8 * n, cudaMemcpyDeviceToHost, st));
+        if (hash_xor) CK(c, cudaMemcpyAsync(hash_xor, c->dbg_hxor, 8 * n, cudaMemcpyDeviceToHost, st));
+        if (acc)
+            CK(c, cudaMemcpyAsync(acc, c->dbg_acc, sizeof(float) * (size_t)c->dim * n, cudaMemcpyDeviceToHost, st));
+    }
+    CK(c, cudaMemcpyAsync(&cand, c->dbg_cand, sizeof(cand), cudaMemcpyDeviceToHost, st));
+    CK(c, cudaStreamSynchronize(st));
+    if (candidates) *candidates = (int64_t)cand;
+    return read_status(c);
+}
+
+int plg_probe_fp32_peak(double* tflops) {
+    if (!tflops) return PLG_E_INVALID_ARG;
+    cudaError_t e = probe_fp32_peak(tflops);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return PLG_E_CUDA;
+    }
+    return PLG_OK;
+}
+
+}  // extern "C"

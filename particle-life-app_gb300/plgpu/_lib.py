@@ -1,0 +1,123 @@
+"""ctypes binding of libplgpu.so (the C ABI of include/plgpu.h).
+
+Loading fails loudly when the library is missing: there is no CPU fallback
+for the physics step.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+import numpy as np
+
+from . import _build
+
+PLG_OK = 0
+PLG_E_INVALID_ARG = 1
+PLG_E_UNSUPPORTED = 2
+PLG_E_STATE = 3
+PLG_E_NO_MEMORY = 4
+PLG_E_CUDA = 5
+PLG_E_TIMEOUT = 6
+PLG_E_STOPPED = 7
+PLG_E_DEVICE = 8
+PLG_E_CAPACITY = 9
+
+PLG_ACCEL_PARTICLE_LIFE = 1
+
+KERNELS = ["scan_reduce", "scan_parts", "scan_down", "scatter", "gather", "force"]
+
+
+class plg_settings(C.Structure):
+    _fields_ = [
+        ("rmax", C.c_double),
+        ("friction", C.c_double),
+        ("force", C.c_double),
+        ("dt", C.c_double),
+        ("beta", C.c_double),
+        ("wrap", C.c_int32),
+        ("accel_kind", C.c_int32),
+    ]
+
+
+class PlgError(RuntimeError):
+    """A plg_* call returned a non-zero status."""
+
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{message} (status {status})")
+        self.status = status
+
+
+_P = C.c_void_p
+_I32P = C.POINTER(C.c_int32)
+_I64P = C.POINTER(C.c_int64)
+_DP = C.POINTER(C.c_double)
+_FP = C.POINTER(C.c_float)
+_U64P = C.POINTER(C.c_uint64)
+
+# name -> (restype, argtypes)
+SIGNATURES = {
+    "plg_version": (C.c_char_p, []),
+    "plg_status_string": (C.c_char_p, [C.c_int]),
+    "plg_validate_settings": (C.c_int, [C.c_int, C.POINTER(plg_settings)]),
+    "plg_cell_bounds": (C.c_int, [C.c_double, _I32P, _FP, C.c_int64]),
+    "plg_create": (C.c_int, [C.c_int, C.c_int64, C.POINTER(_P)]),
+    "plg_destroy": (C.c_int, [_P]),
+    "plg_set_settings": (C.c_int, [_P, C.POINTER(plg_settings)]),
+    "plg_get_settings": (C.c_int, [_P, C.POINTER(plg_settings)]),
+    "plg_set_matrix": (C.c_int, [_P, C.c_int32, _DP]),
+    "plg_upload": (C.c_int, [_P, C.c_int64, _DP, _DP, _I32P]),
+    "plg_step": (C.c_int, [_P, C.c_int32]),
+    "plg_step_async": (C.c_int, [_P, C.c_int32]),
+    "plg_sync": (C.c_int, [_P, C.c_double]),
+    "plg_download": (C.c_int, [_P, _DP, _DP, _I32P, _I32P]),
+    "plg_particle_count": (C.c_int, [_P, _I64P]),
+    "plg_request_stop": (C.c_int, [_P]),
+    "plg_last_error": (C.c_char_p, [_P]),
+    "plg_get_stream": (C.c_int, [_P, C.POINTER(_P)]),
+    "plg_set_use_graph": (C.c_int, [_P, C.c_int32]),
+    "plg_profile_enable": (C.c_int, [_P, C.c_int32]),
+    "plg_profile_read": (C.c_int, [_P, C.c_int32, _DP, _I64P]),
+    "plg_kernel_name": (C.c_char_p, [C.c_int32]),
+    "plg_debug_step": (C.c_int, [_P, _I32P, _I32P, _U64P, _U64P, _FP, _I64P]),
+    "plg_probe_fp32_peak": (C.c_int, [_DP]),
+}
+
+_lib = None
+
+
+def library_path() -> Path:
+    return Path(os.environ.get("PLGPU_LIB", _build.LIB_PATH))
+
+
+def load(build_if_missing: bool = True) -> C.CDLL:
+    """Loads libplgpu.so (building it first if it is absent)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = library_path()
+    if not path.exists():
+        if not build_if_missing:
+            raise RuntimeError(f"{path} is missing: build it with plgpu._build.build()")
+        _build.build()
+    lib = C.CDLL(str(path))
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def ptr(a: np.ndarray | None, ctype):
+    """ctypes pointer to a C-contiguous numpy array (or NULL)."""
+    if a is None:
+        return None
+    if not a.flags["C_CONTIGUOUS"]:
+        raise ValueError("array must be C-contiguous")
+    return a.ctypes.data_as(C.POINTER(ctype))
+
+
+def status_string(status: int) -> str:
+    return load().plg_status_string(status).decode()

@@ -1,0 +1,569 @@
+"""Host-side mirror of the reference's physics API over the GPU C ABI.
+
+Same names, argument meanings and error behaviour as the Java backend of
+tom-mohr/particle-life-app (paths relative to
+src/main/java/com/particle_life/backend/):
+
+  PhysicsSettings  PhysicsSettings.java:8-72
+  Matrix           Matrix.java:3-8, DefaultMatrix.java:3-69
+  Accelerator      Accelerator.java:16 (+ the default lambda, app/Main.java:275-280)
+  PositionSetter / TypeSetter / MatrixGenerator   PositionSetter.java:6,
+                   TypeSetter.java:14, MatrixGenerator.java:9 and their
+                   Default* implementations
+  Physics          Physics.java:9-512
+
+Particles are held as arrays (the structure-of-arrays view of
+``Particle[]``): ``positions`` and ``velocities`` are float64 (n, 3), ``types``
+int32 (n,), ``ids`` int32 (n,).  ``update()`` runs the step on the GPU: the
+host state is uploaded when a mutator touched it, one step runs, and the new
+state (in the new cell-sorted order, as ``Physics.particles`` is permuted by
+every update) is read back according to ``sync_policy``.
+
+Only :class:`ParticleLifeAccelerator` has a device implementation; any other
+accelerator makes ``update()`` raise (no CPU fallback).
+"""
+from __future__ import annotations
+
+import copy
+import math
+from dataclasses import dataclass, field
+from typing import Callable, Optional, Protocol
+
+import numpy as np
+
+from . import _lib
+
+
+# ---------------------------------------------------------------- matrix --
+
+
+class Matrix(Protocol):
+    """backend/Matrix.java:3-8."""
+
+    def size(self) -> int: ...
+
+    def get(self, i: int, j: int) -> float: ...
+
+    def set(self, i: int, j: int, value: float) -> None: ...
+
+    def deep_copy(self) -> "Matrix": ...
+
+
+class DefaultMatrix:
+    """backend/DefaultMatrix.java: n x n doubles, zero-initialised."""
+
+    def __init__(self, size: int):
+        self.values = np.zeros((size, size), dtype=np.float64)
+
+    @property
+    def size_(self) -> int:
+        return self.values.shape[0]
+
+    def size(self) -> int:
+        return self.values.shape[0]
+
+    def zero(self) -> None:
+        self.values[:] = 0.0
+
+    def randomize(self, rng: np.random.Generator) -> None:
+        """values[i][j] = 2 * random() - 1 (DefaultMatrix.java:25-31), seeded."""
+        self.values[:] = 2.0 * rng.random(self.values.shape) - 1.0
+
+    def get(self, i: int, j: int) -> float:
+        return float(self.values[i, j])
+
+    def set(self, i: int, j: int, value: float) -> None:
+        self.values[i, j] = value
+
+    def deep_copy(self) -> "DefaultMatrix":
+        m = DefaultMatrix(self.size())
+        m.values[:] = self.values
+        return m
+
+    def __eq__(self, other) -> bool:
+        if not hasattr(other, "size") or other.size() != self.size():
+            return False
+        n = self.size()
+        return all(other.get(i, j) == self.get(i, j) for i in range(n) for j in range(n))
+
+    def as_array(self) -> np.ndarray:
+        return np.ascontiguousarray(self.values, dtype=np.float64)
+
+
+def matrix_to_array(m) -> np.ndarray:
+    if isinstance(m, DefaultMatrix):
+        return m.as_array()
+    n = m.size()
+    return np.array([[m.get(i, j) for j in range(n)] for i in range(n)], dtype=np.float64)
+
+
+# -------------------------------------------------------------- settings --
+
+# `public double dt = 0.02f;` (PhysicsSettings.java:37): a float literal.
+DEFAULT_DT = float(np.float32(0.02))
+
+
+@dataclass
+class PhysicsSettings:
+    """backend/PhysicsSettings.java:8-38."""
+
+    wrap: bool = True
+    rmax: float = 0.02
+    friction: float = 0.85
+    force: float = 1.0
+    dt: float = DEFAULT_DT
+    matrix: object = field(default_factory=lambda: DefaultMatrix(6))
+
+    def deep_copy(self) -> "PhysicsSettings":
+        return PhysicsSettings(self.wrap, self.rmax, self.friction, self.force, self.dt, self.matrix.deep_copy())
+
+    def __eq__(self, o) -> bool:
+        if not isinstance(o, PhysicsSettings):
+            return False
+        return (
+            o.wrap == self.wrap
+            and o.rmax == self.rmax
+            and o.friction == self.friction
+            and o.force == self.force
+            and o.dt == self.dt
+            and o.matrix == self.matrix
+        )
+
+
+# ----------------------------------------------------------- accelerator --
+
+
+class Accelerator(Protocol):
+    """backend/Accelerator.java:16: acceleration for matrix entry a and r/rmax."""
+
+    def accelerate(self, a: float, pos: np.ndarray) -> np.ndarray: ...
+
+
+@dataclass(frozen=True)
+class ParticleLifeAccelerator:
+    """The default lambda of app/Main.java:275-280, with beta as a parameter.
+
+    ``accelerate`` evaluates it on the host for callers that want the value;
+    the GPU step uses the same formula in its force kernel.
+    """
+
+    beta: float = 0.3
+
+    def accelerate(self, a: float, pos: np.ndarray) -> np.ndarray:
+        pos = np.asarray(pos, dtype=np.float64)
+        dist = math.sqrt(pos[0] * pos[0] + (pos[1] * pos[1] + pos[2] * pos[2]))
+        beta = self.beta
+        f = (dist / beta - 1) if dist < beta else a * (1 - abs(1 + beta - 2 * dist) / (1 - beta))
+        return pos * (f / dist)
+
+
+# ---------------------------------------------------- setters / generator --
+
+
+class PositionSetter(Protocol):
+    def set(self, position: np.ndarray, type_: int, n_types: int) -> None: ...
+
+
+class TypeSetter(Protocol):
+    def get_type(self, position: np.ndarray, velocity: np.ndarray, type_: int, n_types: int) -> int: ...
+
+
+class MatrixGenerator(Protocol):
+    def make_matrix(self, size: int): ...
+
+
+class DefaultPositionSetter:
+    """DefaultPositionSetter.java: uniform in [0,1)^2 (z = 0), seeded here."""
+
+    def __init__(self, rng: np.random.Generator, dim: int = 2):
+        self.rng = rng
+        self.dim = dim
+
+    def set(self, position: np.ndarray, type_: int, n_types: int) -> None:
+        position[0] = self.rng.random()
+        position[1] = self.rng.random()
+        position[2] = self.rng.random() if self.dim == 3 else 0.0
+
+
+class DefaultTypeSetter:
+    """DefaultTypeSetter.java: floor(random() * nTypes), seeded here."""
+
+    def __init__(self, rng: np.random.Generator):
+        self.rng = rng
+
+    def get_type(self, position, velocity, type_: int, n_types: int) -> int:
+        return int(math.floor(self.rng.random() * n_types))
+
+
+class DefaultMatrixGenerator:
+    """DefaultMatrixGenerator.java: a randomized DefaultMatrix."""
+
+    def __init__(self, rng: np.random.Generator):
+        self.rng = rng
+
+    def make_matrix(self, size: int) -> DefaultMatrix:
+        m = DefaultMatrix(size)
+        m.randomize(self.rng)
+        return m
+
+
+# ---------------------------------------------------------------- world --
+
+
+def check(status: int, ctx=None, what: str = "") -> None:
+    if status != _lib.PLG_OK:
+        lib = _lib.load()
+        msg = lib.plg_last_error(ctx).decode() if ctx else ""
+        raise _lib.PlgError(status, f"{what}: {lib.plg_status_string(status).decode()}: {msg}")
+
+
+class GpuWorld:
+    """Thin owner of one plg_ctx (one world on the current CUDA device)."""
+
+    def __init__(self, dim: int, capacity: int):
+        self.lib = _lib.load()
+        self.dim = dim
+        self.capacity = int(capacity)
+        h = _lib.C.c_void_p()
+        check(self.lib.plg_create(dim, self.capacity, _lib.C.byref(h)), None, "plg_create")
+        self.ctx = h
+
+    def close(self) -> None:
+        if getattr(self, "ctx", None):
+            self.lib.plg_destroy(self.ctx)
+            self.ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _c(self, status: int, what: str) -> None:
+        check(status, self.ctx, what)
+
+    def set_settings(self, rmax, friction, force, dt, beta=0.3, wrap=True, accel_kind=_lib.PLG_ACCEL_PARTICLE_LIFE):
+        s = _lib.plg_settings(rmax, friction, force, dt, beta, 1 if wrap else 0, accel_kind)
+        self._c(self.lib.plg_set_settings(self.ctx, _lib.C.byref(s)), "plg_set_settings")
+
+    def set_matrix(self, m: np.ndarray) -> None:
+        m = np.ascontiguousarray(m, dtype=np.float64)
+        self._c(self.lib.plg_set_matrix(self.ctx, m.shape[0], _lib.ptr(m, _lib.C.c_double)), "plg_set_matrix")
+
+    def upload(self, pos: np.ndarray, vel: Optional[np.ndarray], types: np.ndarray) -> None:
+        pos = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1, 3)
+        n = pos.shape[0]
+        velp = None
+        if vel is not None:
+            vel = np.ascontiguousarray(vel, dtype=np.float64).reshape(-1, 3)
+            velp = _lib.ptr(vel, _lib.C.c_double)
+        types = np.ascontiguousarray(types, dtype=np.int32)
+        self._c(
+            self.lib.plg_upload(self.ctx, n, _lib.ptr(pos, _lib.C.c_double), velp, _lib.ptr(types, _lib.C.c_int32)),
+            "plg_upload",
+        )
+
+    def step(self, n: int = 1) -> None:
+        self._c(self.lib.plg_step(self.ctx, n), "plg_step")
+
+    def count(self) -> int:
+        v = _lib.C.c_int64()
+        self._c(self.lib.plg_particle_count(self.ctx, _lib.C.byref(v)), "plg_particle_count")
+        return v.value
+
+    def download(self):
+        n = self.count()
+        pos = np.empty((n, 3), np.float64)
+        vel = np.empty((n, 3), np.float64)
+        types = np.empty(n, np.int32)
+        ids = np.empty(n, np.int32)
+        self._c(
+            self.lib.plg_download(
+                self.ctx,
+                _lib.ptr(pos, _lib.C.c_double),
+                _lib.ptr(vel, _lib.C.c_double),
+                _lib.ptr(types, _lib.C.c_int32),
+                _lib.ptr(ids, _lib.C.c_int32),
+            ),
+            "plg_download",
+        )
+        return pos, vel, types, ids
+
+    def debug_step(self):
+        """One step with the instrumented kernel: per-particle cell, pair
+        count, pair hashes, FP32 accelerations (cell-sorted order)."""
+        n = self.count()
+        cell = np.empty(n, np.int32)
+        pairs = np.empty(n, np.int32)
+        hs = np.empty(n, np.uint64)
+        hx = np.empty(n, np.uint64)
+        acc = np.empty((n, self.dim), np.float32)
+        cand = _lib.C.c_int64()
+        self._c(
+            self.lib.plg_debug_step(
+                self.ctx,
+                _lib.ptr(cell, _lib.C.c_int32),
+                _lib.ptr(pairs, _lib.C.c_int32),
+                _lib.ptr(hs, _lib.C.c_uint64),
+                _lib.ptr(hx, _lib.C.c_uint64),
+                _lib.ptr(acc, _lib.C.c_float),
+                _lib.C.byref(cand),
+            ),
+            "plg_debug_step",
+        )
+        return dict(cell=cell, pairs=pairs, hsum=hs, hxor=hx, acc=acc, candidates=cand.value)
+
+    def request_stop(self) -> None:
+        self._c(self.lib.plg_request_stop(self.ctx), "plg_request_stop")
+
+    def stream(self) -> int:
+        p = _lib.C.c_void_p()
+        self._c(self.lib.plg_get_stream(self.ctx, _lib.C.byref(p)), "plg_get_stream")
+        return p.value or 0
+
+
+class Physics:
+    """Mirror of com.particle_life.backend.Physics (Physics.java:9-512).
+
+    ``dim`` = 3 selects the project's 3D extension (27-cell stencil); the
+    reference itself is 2D.  Construction only touches the host: the GPU
+    world is created on the first ``update()``.
+    """
+
+    DEFAULT_MATRIX_SIZE = 7
+
+    def __init__(
+        self,
+        accelerator,
+        position_setter=None,
+        matrix_generator=None,
+        type_setter=None,
+        *,
+        dim: int = 2,
+        seed: int = 0,
+        initial_count: int = 10000,
+        capacity: Optional[int] = None,
+        sync_policy: str = "every",
+    ):
+        self.rng = np.random.Generator(np.random.Philox(seed))
+        self.dim = dim
+        self.settings = PhysicsSettings()
+        self.accelerator = accelerator
+        self.position_setter = position_setter or DefaultPositionSetter(self.rng, dim)
+        self.matrix_generator = matrix_generator or DefaultMatrixGenerator(self.rng)
+        self.type_setter = type_setter or DefaultTypeSetter(self.rng)
+        self.preferred_number_of_threads = 12  # kept for API parity; unused on the GPU
+        self.sync_policy = sync_policy
+        self.capacity = capacity
+        self.positions = np.zeros((0, 3), np.float64)
+        self.velocities = np.zeros((0, 3), np.float64)
+        self.types = np.zeros(0, np.int32)
+        self.ids = np.zeros(0, np.int32)
+        self._world: Optional[GpuWorld] = None
+        self._host_dirty = True
+        self._device_newer = False
+        self._pushed: Optional[tuple] = None
+        self._pushed_matrix: Optional[np.ndarray] = None
+        self.generate_matrix()
+        self.set_particle_count(initial_count)
+
+    # -- control (Physics.java:149-170) --
+
+    def force_update_stop(self) -> None:
+        if self._world is not None:
+            self._world.request_stop()
+
+    def kill(self) -> None:
+        self.force_update_stop()
+
+    def set_positions(self) -> None:
+        self._sync_host()
+        for i in range(len(self.types)):
+            self._set_position(i)
+        self._host_dirty = True
+
+    def generate_matrix(self) -> None:
+        prev = self.settings.matrix.size() if self.settings.matrix is not None else self.DEFAULT_MATRIX_SIZE
+        self.settings.matrix = self.matrix_generator.make_matrix(prev)
+        assert self.settings.matrix.size() == prev, "Matrix size should only change via setMatrixSize()"
+
+    def set_particle_count(self, n: int) -> None:
+        """Physics.java:190-223: shrink keeps a random subset, grow appends
+        particles made by the type and position setters."""
+        if n < 0:
+            raise ValueError("n must be 0 or greater")
+        self._sync_host()
+        cur = len(self.types)
+        if n < cur:
+            order = self.rng.permutation(cur)
+            keep = order[:n]
+            self.positions = self.positions[keep].copy()
+            self.velocities = self.velocities[keep].copy()
+            self.types = self.types[keep].copy()
+            self.ids = self.ids[keep].copy()
+        elif n > cur:
+            add = n - cur
+            pos = np.zeros((add, 3), np.float64)
+            vel = np.zeros((add, 3), np.float64)
+            typ = np.zeros(add, np.int32)
+            self.positions = np.concatenate([self.positions, pos])
+            self.velocities = np.concatenate([self.velocities, vel])
+            self.types = np.concatenate([self.types, typ])
+            start = int(self.ids.max()) + 1 if len(self.ids) else 0
+            self.ids = np.concatenate([self.ids, np.arange(start, start + add, dtype=np.int32)])
+            for i in range(cur, n):
+                self._set_type(i)
+                self._set_position(i)
+        self._host_dirty = True
+
+    def set_matrix_size(self, new_size: int) -> None:
+        """Physics.java:238-258."""
+        prev = self.settings.matrix
+        prev_size = prev.size()
+        if new_size == prev_size:
+            return
+        self.settings.matrix = self.matrix_generator.make_matrix(new_size)
+        assert self.settings.matrix.size() == new_size
+        common = min(prev_size, new_size)
+        for i in range(common):
+            for j in range(common):
+                self.settings.matrix.set(i, j, prev.get(i, j))
+        if new_size < prev_size:
+            self.ensure_types()
+
+    def ensure_types(self) -> None:
+        """Physics.java:266-272."""
+        self._sync_host()
+        n = self.settings.matrix.size()
+        for i in np.nonzero(self.types >= n)[0]:
+            self._set_type(int(i))
+        self._host_dirty = True
+
+    def set_types(self) -> None:
+        """Physics.java:509-511."""
+        self._sync_host()
+        for i in range(len(self.types)):
+            self._set_type(i)
+        self._host_dirty = True
+
+    # -- protected setters (Physics.java:297-307) --
+
+    def _set_position(self, i: int) -> None:
+        p = self.positions[i]
+        self.position_setter.set(p, int(self.types[i]), self.settings.matrix.size())
+        self.ensure_position(p)
+        self.velocities[i] = 0.0
+
+    def _set_type(self, i: int) -> None:
+        self.types[i] = self.type_setter.get_type(
+            self.positions[i].copy(), self.velocities[i].copy(), int(self.types[i]), self.settings.matrix.size()
+        )
+
+    # -- geometry helpers (Physics.java:460-505) --
+
+    def connection(self, pos1, pos2) -> np.ndarray:
+        delta = np.asarray(pos2, np.float64) - np.asarray(pos1, np.float64)
+        if self.settings.wrap:
+            for k in range(3):
+                v = delta[k]
+                delta[k] = v + 1 if v < -0.5 else (v - 1 if v >= 0.5 else v)
+            if self.dim == 2:
+                delta[2] = 0.0
+        return delta
+
+    def distance(self, pos1, pos2) -> float:
+        d = self.connection(pos1, pos2)
+        return math.sqrt(d[0] * d[0] + (d[1] * d[1] + d[2] * d[2]))
+
+    def ensure_position(self, position: np.ndarray) -> None:
+        dims = 3 if self.dim == 3 else 2
+        for k in range(dims):
+            v = float(position[k])
+            if self.settings.wrap:
+                if v < 0:
+                    while True:
+                        v += 1
+                        if not v < 0:
+                            break
+                else:
+                    while v >= 1:
+                        v -= 1
+            else:
+                v = 0.0 if v < 0 else (1.0 if v > 1 else v)
+            position[k] = v
+        if self.dim == 2:
+            position[2] = 0.0
+
+    # -- the step (Physics.java:112-134) --
+
+    @property
+    def world(self) -> GpuWorld:
+        if self._world is None:
+            cap = max(self.capacity or 0, len(self.types), 1)
+            self._world = GpuWorld(self.dim, cap)
+        return self._world
+
+    def _beta(self) -> float:
+        if not isinstance(self.accelerator, ParticleLifeAccelerator):
+            raise _lib.PlgError(
+                _lib.PLG_E_UNSUPPORTED,
+                "only ParticleLifeAccelerator has a GPU implementation; there is no CPU fallback",
+            )
+        return self.accelerator.beta
+
+    def _push(self) -> None:
+        w = self.world
+        if len(self.types) > w.capacity:
+            w.close()
+            self._world = None
+            self._pushed = None
+            self._pushed_matrix = None
+            w = self.world
+        s = self.settings
+        key = (s.wrap, s.rmax, s.friction, s.force, s.dt, self._beta())
+        if key != self._pushed:
+            w.set_settings(s.rmax, s.friction, s.force, s.dt, beta=key[5], wrap=s.wrap)
+            self._pushed = key
+        m = matrix_to_array(s.matrix)
+        pm = self._pushed_matrix
+        if pm is None or m.shape != pm.shape or not np.array_equal(m, pm):
+            if pm is not None and m.shape != pm.shape:
+                self._sync_host()
+                self._host_dirty = True
+            try:
+                w.set_matrix(m)
+            except _lib.PlgError as e:
+                # A shrink below the uploaded types invalidates the device
+                # state; the re-upload below validates the host types.
+                if e.status != _lib.PLG_E_STATE:
+                    raise
+            self._pushed_matrix = m
+        if self._host_dirty:
+            w.upload(self.positions, self.velocities, self.types)
+            self._device_ids = self.ids.copy()
+            self._host_dirty = False
+
+    def update(self) -> None:
+        """One Physics.update() on the GPU."""
+        self._push()
+        self.world.step(1)
+        self._device_newer = True
+        if self.sync_policy == "every":
+            self._sync_host()
+
+    def _sync_host(self) -> None:
+        if not self._device_newer or self._world is None:
+            return
+        pos, vel, types, ids = self._world.download()
+        self.positions, self.velocities, self.types = pos, vel, types
+        self.ids = self._device_ids[ids]
+        self._device_newer = False
+
+    def sync_host(self) -> None:
+        """Brings the host arrays up to date (for sync_policy='manual')."""
+        self._sync_host()
+
+    def close(self) -> None:
+        if self._world is not None:
+            self._world.close()
+            self._world = None

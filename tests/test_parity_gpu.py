@@ -1,0 +1,148 @@
+"""GPU parity: one instrumented step through the C ABI against the FP64 oracle.
+
+Bit-exact: the sorted order (particle ids after the step), the cell of every
+particle, and each particle's interacting-pair set (count, sum and xor of
+splitmix64(id)).  Floating point, on the same FP32 start state:
+  - accelerations (sum of Accelerator.accelerate terms): norm-wise relative
+    error <= 1e-5, and per particle |a - a*| / sum_j |term_j| <= 1e-5;
+  - velocities after the step: norm-wise relative error <= 1e-5;
+  - positions after the step: max periodic distance <= 2e-7 (FP32 rounding of
+    a coordinate in [0,1) is <= 6e-8).
+"""
+import numpy as np
+import pytest
+
+from worlds import (FRICTION_T_HALF_0043, WorldSpec, accel_errors, blob_world, f32, min_image, norm_rel,
+                    run_gpu_debug, run_oracle_debug, uniform_world)
+
+pytestmark = pytest.mark.gpu
+
+ACC_TOL = 1e-5
+VEL_TOL = 1e-5
+POS_TOL = 2e-7
+
+
+def check_step(spec: WorldSpec, gpu, exact_only=False):
+    g, (gpos, gvel, gtypes, gids) = run_gpu_debug(spec)
+    d, o = run_oracle_debug(spec)
+    assert np.array_equal(gids, o.ids), "sorted order (ids) differs from the oracle"
+    assert np.array_equal(gtypes, o.types)
+    assert np.array_equal(g["cell"], d["cell"]), "cell assignment differs"
+    assert np.array_equal(g["pairs"], d["pairs"]), "interacting-pair counts differ"
+    assert np.array_equal(g["hsum"], d["hsum"]), "interacting-pair sets differ (sum hash)"
+    assert np.array_equal(g["hxor"], d["hxor"]), "interacting-pair sets differ (xor hash)"
+    out = dict(pairs=float(d["pairs"].mean()) if spec.n else 0.0)
+    if spec.n == 0 or d["pairs"].sum() == 0 or exact_only:
+        return out
+    acc_g = g["acc"].astype(np.float64)
+    e = accel_errors(acc_g, d["acc"])
+    assert e["normwise"] <= ACC_TOL, e
+    scale = np.where(d["accabs"] > 0, d["accabs"], 1.0)
+    per = np.linalg.norm(acc_g - d["acc"], axis=1) / scale
+    assert per.max() <= ACC_TOL, per.max()
+    dim = spec.dim
+    assert norm_rel(gvel[:, :dim], o.vel[:, :dim]) <= VEL_TOL
+    dp = min_image(gpos[:, :dim] - o.pos[:, :dim], spec.wrap)
+    assert np.abs(dp).max() <= POS_TOL, np.abs(dp).max()
+    out.update(e)
+    return out
+
+
+def test_cfg1_2d_10k(gpu):
+    check_step(uniform_world(10_000, 6, 0.02, seed=1, vel_scale=0.01, dt=0.02), gpu)
+
+
+def test_cfg2_2d_1m(gpu):
+    r = check_step(uniform_world(1_000_000, 8, 0.0025, seed=2, vel_scale=0.01, dt=0.01), gpu)
+    assert 18 < r["pairs"] < 21  # ~19.6 expected neighbours
+
+
+def test_2d_clamp_with_walls(gpu):
+    spec = uniform_world(20_000, 5, 0.01, seed=3, vel_scale=0.05, wrap=False)
+    spec.pos[:200, 0] = 0.0
+    spec.pos[200:400, 0] = 1.0
+    spec.pos[400:600, 1] = 1.0
+    spec.pos[600:800, :2] = 1.0
+    check_step(spec, gpu)
+
+
+def test_2d_last_partial_cell(gpu):
+    """rmax with 1/rmax not an integer: a sliver [nx*cs, 1) beyond the last
+    full cell, whose stencil differs from the binning cell's."""
+    rmax = 0.0031
+    spec = uniform_world(50_000, 4, rmax, seed=4)
+    rng = np.random.Generator(np.random.Philox(44))
+    nx = int(np.floor(1 / rmax))
+    lo = nx * rmax
+    k = 5000
+    spec.pos[:k, 0] = f32(lo + (1 - lo) * rng.random(k))
+    spec.pos[k:2 * k, 1] = f32(lo + (1 - lo) * rng.random(k))
+    spec.pos[2 * k:3 * k, 0] = f32((nx - 2) * rmax + rmax * rng.random(k))  # column nx-2
+    spec.pos[3 * k:3 * k + 500, :2] = f32(lo + (1 - lo) * rng.random((500, 2)))
+    spec.pos[:, :2] = np.minimum(spec.pos[:, :2], np.float64(np.nextafter(np.float32(1), np.float32(0))))
+    check_step(spec, gpu)
+
+
+@pytest.mark.parametrize("rmax", [0.3, 0.4, 0.7])
+def test_2d_small_grids(gpu, rmax):
+    """nx = 3, 2, 1: with nx < 3 the reference visits a cell more than once
+    and counts a pair once per visit."""
+    check_step(uniform_world(1500, 4, rmax, seed=5, vel_scale=0.01), gpu)
+
+
+@pytest.mark.parametrize("wrap", [True, False])
+def test_2d_small_grid_clamp_and_wrap(gpu, wrap):
+    check_step(uniform_world(800, 3, 0.45, seed=6, wrap=wrap), gpu)
+
+
+def test_2d_many_types_matrix_in_global(gpu):
+    check_step(uniform_world(40_000, 100, 0.01, seed=7, vel_scale=0.01), gpu)
+
+
+def test_2d_lattice_at_exactly_rmax(gpu):
+    """Neighbours at exactly rmax (d2 == rmax^2 in FP64) interact (<=);
+    one ulp further they do not."""
+    rmax = 2.0 ** -6
+    k = 64
+    xs = (np.arange(k) * rmax).astype(np.float64)
+    X, Y = np.meshgrid(xs, xs, indexing="ij")
+    pos = np.zeros((k * k, 3))
+    pos[:, 0] = X.ravel()
+    pos[:, 1] = Y.ravel()
+    n = pos.shape[0]
+    rng = np.random.Generator(np.random.Philox(8))
+    spec = WorldSpec(2, pos, np.zeros((n, 3)), rng.integers(0, 3, n).astype(np.int32),
+                     f32(2 * rng.random((3, 3)) - 1), rmax)
+    r = check_step(spec, gpu)
+    assert r["pairs"] == 4.0
+    spec.pos[:, 0] = np.nextafter(spec.pos[:, 0].astype(np.float32) * np.float32(1.0), np.float32(2)).astype(np.float64)
+    check_step(spec, gpu)
+
+
+def test_2d_coincident_particles(gpu):
+    spec = uniform_world(5000, 4, 0.02, seed=9)
+    spec.pos[100:140] = spec.pos[99]
+    spec.pos[1000:1003] = spec.pos[2000]
+    check_step(spec, gpu)
+
+
+def test_2d_fast_particles_wrap_many_times(gpu):
+    spec = uniform_world(5000, 4, 0.02, seed=10)
+    rng = np.random.Generator(np.random.Philox(10))
+    spec.vel[:, :2] = f32(rng.uniform(-400, 400, (spec.n, 2)))
+    check_step(spec, gpu)
+
+
+def test_3d_uniform(gpu):
+    check_step(uniform_world(200_000, 16, 0.02, seed=11, dim=3, vel_scale=0.01, dt=0.01), gpu)
+
+
+def test_3d_blobs_uneven_cells(gpu):
+    """cfg3 shape at 1/10 size: 64 Gaussian blobs, 16 types."""
+    check_step(blob_world(400_000, 16, 0.0095, seed=12, dt=0.01), gpu)
+
+
+def test_empty_and_single(gpu):
+    check_step(uniform_world(0, 3, 0.05, seed=13), gpu)
+    check_step(uniform_world(1, 3, 0.05, seed=13), gpu)
+    check_step(uniform_world(2, 3, 0.5, seed=13), gpu)

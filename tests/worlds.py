@@ -1,0 +1,118 @@
+"""Seeded synthetic worlds and comparison helpers shared by the tests.
+
+Positions, velocities and matrix entries are drawn as float32 and stored as
+float64, so the GPU's FP32 state and the oracle's FP64 state start equal.
+Generators use numpy's Philox4x32 counter-based PRNG (Salmon et al. 2011).
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass
+
+import numpy as np
+
+FRICTION_T_HALF_0043 = 0.5 ** (1.0 / (60.0 * 0.043))  # 0.7644018106552037
+
+
+@dataclass
+class WorldSpec:
+    dim: int
+    pos: np.ndarray  # (n, 3) float64, FP32-exact
+    vel: np.ndarray  # (n, 3) float64, FP32-exact
+    types: np.ndarray  # (n,) int32
+    matrix: np.ndarray  # (t, t) float64, FP32-exact
+    rmax: float
+    friction: float = FRICTION_T_HALF_0043
+    force: float = 1.0
+    dt: float = 0.02
+    beta: float = 0.3
+    wrap: bool = True
+
+    @property
+    def n(self) -> int:
+        return self.pos.shape[0]
+
+
+def rng_of(seed: int) -> np.random.Generator:
+    return np.random.Generator(np.random.Philox(seed))
+
+
+def f32(a) -> np.ndarray:
+    return np.asarray(a, np.float32).astype(np.float64)
+
+
+def uniform_world(n, ntypes, rmax, seed=0, dim=2, vel_scale=0.0, **kw) -> WorldSpec:
+    rng = rng_of(seed)
+    pos = np.zeros((n, 3))
+    pos[:, :dim] = rng.random((n, dim), dtype=np.float32)
+    vel = np.zeros((n, 3))
+    if vel_scale:
+        vel[:, :dim] = f32(rng.standard_normal((n, dim)) * vel_scale)
+    types = rng.integers(0, ntypes, n).astype(np.int32)
+    m = f32(2 * rng.random((ntypes, ntypes)) - 1)
+    return WorldSpec(dim, pos, vel, types, m, rmax, **kw)
+
+
+def blob_world(n, ntypes, rmax, nblobs=64, sigma=0.025, seed=0, dim=3, **kw) -> WorldSpec:
+    """Isotropic Gaussian blobs (sigma in reference units), centres uniform,
+    positions wrapped into the unit box."""
+    rng = rng_of(seed)
+    centres = rng.random((nblobs, dim))
+    which = rng.integers(0, nblobs, n)
+    p = centres[which] + rng.standard_normal((n, dim)) * sigma
+    p = p - np.floor(p)
+    p = np.asarray(p, np.float32)
+    p[p >= 1.0] = 0.0
+    pos = np.zeros((n, 3))
+    pos[:, :dim] = p
+    vel = np.zeros((n, 3))
+    types = rng.integers(0, ntypes, n).astype(np.int32)
+    m = f32(2 * rng.random((ntypes, ntypes)) - 1)
+    return WorldSpec(dim, pos, vel, types, m, rmax, **kw)
+
+
+def min_image(d: np.ndarray, wrap: bool) -> np.ndarray:
+    if not wrap:
+        return d
+    return d - np.round(d)
+
+
+def norm_rel(a: np.ndarray, b: np.ndarray) -> float:
+    nb = np.linalg.norm(b)
+    return float(np.linalg.norm(a - b) / nb) if nb > 0 else float(np.linalg.norm(a - b))
+
+
+def run_gpu_debug(spec: WorldSpec, capacity=None):
+    """Upload spec, run one instrumented step, download; returns (debug, state)."""
+    from plgpu.physics import GpuWorld
+
+    w = GpuWorld(spec.dim, capacity or max(spec.n, 1))
+    try:
+        w.set_settings(spec.rmax, spec.friction, spec.force, spec.dt, beta=spec.beta, wrap=spec.wrap)
+        w.set_matrix(spec.matrix)
+        w.upload(spec.pos, spec.vel, spec.types)
+        d = w.debug_step()
+        st = w.download()
+    finally:
+        w.close()
+    return d, st
+
+
+def run_oracle_debug(spec: WorldSpec, threads=8):
+    import orc
+
+    o = orc.World(spec.dim, spec.pos, spec.vel, spec.types, np.arange(spec.n, dtype=np.int32), spec.matrix,
+                  orc.settings(spec.rmax, spec.friction, spec.force, spec.dt, spec.beta, spec.wrap))
+    d = o.step(threads=threads, debug=True)
+    return d, o
+
+
+def accel_errors(acc_gpu: np.ndarray, acc_ref: np.ndarray, abs_terms: np.ndarray | None = None) -> dict:
+    """Norm-wise relative error and raw per-particle relative error."""
+    e = np.linalg.norm(acc_gpu - acc_ref, axis=1)
+    r = np.linalg.norm(acc_ref, axis=1)
+    nz = r > 0
+    raw = e[nz] / r[nz]
+    out = dict(normwise=norm_rel(acc_gpu, acc_ref))
+    if raw.size:
+        out.update(p50=float(np.percentile(raw, 50)), p99=float(np.percentile(raw, 99)), max=float(raw.max()))
+    return out
