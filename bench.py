@@ -47,7 +47,7 @@ FRICTION = 0.5 ** (1.0 / (60.0 * 0.043))
 FLOPS_PER_CANDIDATE = {2: 6, 3: 9}
 FLOPS_PER_INTERACTION = {2: 13, 3: 15}
 # Bytes each kernel must move per particle / per cell, by design (2D layout).
-BYTES = {"scatter": 12, "gather": 56, "force": 56, "scan_cell": 16}
+BYTES = {"scatter": 12, "gather": 56, "force": 56, "scan_cell": 12}
 
 
 def parse():
@@ -304,7 +304,7 @@ def run_ours(args):
     if hbm:
         cells = (int(np.floor(1 / SETTINGS["rmax"]))) ** 2
         for name, b in (("scatter", BYTES["scatter"] * n), ("gather", BYTES["gather"] * n),
-                        ("scan_down", BYTES["scan_cell"] * cells), ("force", BYTES["force"] * n)):
+                        ("scan", BYTES["scan_cell"] * cells), ("force", BYTES["force"] * n)):
             gbs = b / (kern[name]["avg_us"] * 1e-6) / 1e9
             sort_kernels[name] = {"achieved_gbs": gbs, "frac_of_measured_hbm": gbs / hbm}
 
@@ -329,7 +329,7 @@ def run_ours(args):
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": n * (24 + 24 + 4),
                     "d2h_bytes_per_step": n * (24 + 24 + 4 + 4), "steps": args.e2e_steps,
                     "api": "plg_upload + plg_step + plg_download, pinned host buffers, host wall clock"},
-            "gpu_launches": 6 * args.steps,
+            "gpu_launches": len(_lib.KERNELS) * args.steps,
             "roofline": roofline,
             "kernels": kern,
             "sort_kernels_hbm": sort_kernels,

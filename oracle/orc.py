@@ -56,7 +56,7 @@ class _Debug(C.Structure):
         ("hsum", C.POINTER(C.c_uint64)),
         ("hxor", C.POINTER(C.c_uint64)),
         ("acc", C.POINTER(C.c_double)),
-        ("accabs", C.POINTER(C.c_double)),
+        ("fscale", C.POINTER(C.c_double)),
         ("candidates", C.c_int64),
     ]
 
@@ -128,7 +128,7 @@ class World:
                 hsum=np.zeros(n, np.uint64),
                 hxor=np.zeros(n, np.uint64),
                 acc=np.zeros((n, self.dim), np.float64),
-                accabs=np.zeros(n, np.float64),
+                fscale=np.zeros(n, np.float64),
             )
             dbg = _Debug(
                 _p(out["cell"], C.c_int32),
@@ -136,7 +136,7 @@ class World:
                 _p(out["hsum"], C.c_uint64),
                 _p(out["hxor"], C.c_uint64),
                 _p(out["acc"], C.c_double),
-                _p(out["accabs"], C.c_double),
+                _p(out["fscale"], C.c_double),
                 0,
             )
         rc = lib.orc_step(self.dim, n, _p(self.pos, C.c_double), _p(self.vel, C.c_double), _p(self.types, C.c_int32),

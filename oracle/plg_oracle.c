@@ -57,7 +57,10 @@ typedef struct orc_debug {
     uint64_t* hsum;    /* sum of mix64(id) of interacting partners          */
     uint64_t* hxor;    /* xor of mix64(id)                                  */
     double* acc;       /* dim * n: sum of accelerate(a, r / rmax)           */
-    double* accabs;    /* sum of |accelerate(a, r / rmax)| (error scale)    */
+    double* fscale;    /* sum over interacting pairs of max(1, |a_ij|): the
+                          bound of each term's magnitude |f| and so the
+                          scale of its rounding error (f itself vanishes at
+                          r = beta and r = 1, so |term| is no error scale) */
     int64_t candidates;/* out: pairs tested (j != i)                        */
 } orc_debug;
 
@@ -247,7 +250,7 @@ static void update_velocity(world* w, int64_t i, int64_t* cand) {
     int32_t npairs = 0;
     uint64_t hs = 0, hx = 0;
     double acc[3] = {0, 0, 0};
-    double accabs = 0;
+    double fscale = 0;
 
     for (int oz = zlo; oz <= zhi; oz++) {
         for (int oy = -1; oy <= 1; oy++) {
@@ -290,7 +293,7 @@ static void update_velocity(world* w, int64_t i, int64_t* cand) {
                         acc[0] += dv[0];
                         acc[1] += dv[1];
                         acc[2] += dv[2];
-                        accabs += sqrt(dv[0] * dv[0] + dv[1] * dv[1] + dv[2] * dv[2]);
+                        fscale += fabs(a) > 1 ? fabs(a) : 1.0;
                         v[0] = v[0] + dv[0] * scale;
                         v[1] = v[1] + dv[1] * scale;
                         v[2] = v[2] + dv[2] * scale;
@@ -310,7 +313,7 @@ static void update_velocity(world* w, int64_t i, int64_t* cand) {
         if (w->dbg->acc) {
             for (int k = 0; k < dim; k++) w->dbg->acc[(int64_t)dim * i + k] = acc[k];
         }
-        if (w->dbg->accabs) w->dbg->accabs[i] = accabs;
+        if (w->dbg->fscale) w->dbg->fscale[i] = fscale;
     }
 }
 

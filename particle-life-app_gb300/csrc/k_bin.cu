@@ -4,15 +4,19 @@
 // Per step (after the force kernel of the previous step, or the upload, has
 // written every particle's cell and an in-cell rank and bumped the per-cell
 // counts):
-//   scan_reduce / scan_parts / scan_down  counts -> exclusive offsets
-//                                         (Physics.java:334-340); counts reset
+//   scan      counts -> exclusive offsets (Physics.java:334-340), single
+//             pass with decoupled look-back; counts reset
 //   scatter   perm[cstart[cell]+rank] = i (unstable: atomics order warps)
-//   gather    rank_stable(i) = #{members of i's cell with a smaller index};
-//             B[cstart[cell] + rank_stable] = A[i]
-// The gather makes the sort stable, so the cell-sorted order equals the one
-// the reference's sequential scatter (Physics.java:342-348) produces.  The
-// stable re-rank costs sum_c n_c^2 compares, a ninth of the force loop's
-// sum_c n_c * (9 neighbour cells) candidate tests.
+//   gather    rank_stable(i) = #{members of i's cell with a smaller index},
+//             rank_x(i) = #{members before i in (x, index) order};
+//             B[cstart[cell] + rank_x] = A[i],
+//             refslot[cstart[cell] + rank_x] = cstart[cell] + rank_stable
+// The stable rank reproduces the order of the reference's sequential
+// scatter (Physics.java:342-348): the force kernel writes each particle's
+// next state to A[refslot[slot]], so A always holds the reference's order.
+// The x order inside B lets the force kernel cut each candidate run to the
+// |dx| <= rmax window.  The re-ranks cost sum_c n_c^2 compares, a ninth of
+// the force loop's sum_c n_c * (9 neighbour cells) candidate tests.
 #include "plg_internal.cuh"
 
 namespace plg {
@@ -20,7 +24,7 @@ namespace plg {
 namespace {
 
 constexpr int kThreads = 256;
-constexpr int kScanThreads = 1024;
+constexpr int kScanThreads = 256;
 constexpr int kScanItems = 4;
 constexpr int kScanTile = kScanThreads * kScanItems;
 
@@ -150,10 +154,11 @@ __device__ __forceinline__ uint32_t block_exclusive(uint32_t v, uint32_t* total)
     const uint32_t inc = warp_inclusive(v);
     if (lane == 31) warp_sums[warp] = inc;
     __syncthreads();
-    if (warp == 0) {  // kScanThreads / 32 == 32 warp sums, one per lane
-        const uint32_t s = warp_sums[lane];
+    if (warp == 0) {
+        constexpr int kWarps = kScanThreads / 32;
+        const uint32_t s = lane < kWarps ? warp_sums[lane] : 0u;
         const uint32_t si = warp_inclusive(s);
-        warp_sums[lane] = si - s;
+        if (lane < kWarps) warp_sums[lane] = si - s;
         if (lane == 31) *total = si;
     }
     __syncthreads();
@@ -162,67 +167,105 @@ __device__ __forceinline__ uint32_t block_exclusive(uint32_t v, uint32_t* total)
     return r;
 }
 
-__global__ void __launch_bounds__(kScanThreads) k_scan_reduce(const uint32_t* __restrict__ counts, int ncells,
-                                                              uint32_t* __restrict__ parts) {
-    const int base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
-    uint32_t s = 0;
-#pragma unroll
-    for (int k = 0; k < kScanItems; ++k) {
-        if (base + k < ncells) s += counts[base + k];
-    }
-    __shared__ uint32_t red[kScanThreads / 32];
-#pragma unroll
-    for (int d = 16; d > 0; d >>= 1) s += __shfl_down_sync(kFull, s, d);
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
-    __syncthreads();
-    if (threadIdx.x < 32) {
-        uint32_t t = red[threadIdx.x];
-#pragma unroll
-        for (int d = 16; d > 0; d >>= 1) t += __shfl_down_sync(kFull, t, d);
-        if (threadIdx.x == 0) parts[blockIdx.x] = t;
-    }
+constexpr unsigned long long kTileAggregate = 1ull << 32;  // status word: tile sum published
+constexpr unsigned long long kTileInclusive = 2ull << 32;  // status word: prefix through tile
+constexpr int kLookbackSpinLimit = 1 << 22;
+
+__device__ __forceinline__ unsigned long long load_volatile(const unsigned long long* p) {
+    return *reinterpret_cast<const volatile unsigned long long*>(p);
 }
 
-// One block: exclusive scan of the per-tile sums, in place.
-__global__ void __launch_bounds__(kScanThreads) k_scan_parts(uint32_t* parts, int nparts) {
-    __shared__ uint32_t carry_s;
-    __shared__ uint32_t total;
-    if (threadIdx.x == 0) carry_s = 0;
+// Single-pass exclusive scan of the per-cell counts (capacity -> index,
+// Physics.java:334-340) with decoupled look-back: each block takes the next
+// tile id, publishes its tile sum, and adds the sums of earlier tiles until it
+// meets a published inclusive prefix.  Tile ids follow block start order, so
+// a block only waits on blocks that are already running; every wait is
+// bounded and raises kDevSpinLimit instead of hanging.  Counts are reset to
+// zero for the next counting pass.  state[0] is the tile counter and
+// state[1 + t] the status word of tile t; both start at zero each step.
+__global__ void __launch_bounds__(kScanThreads) k_scan(uint32_t* __restrict__ counts, int ncells,
+                                                       uint32_t* __restrict__ cstart, unsigned long long* state,
+                                                       uint32_t* status, uint32_t* zero_word) {
+    __shared__ uint32_t s_tile, s_prefix, total;
+    if (threadIdx.x == 0) s_tile = atomicAdd(reinterpret_cast<unsigned int*>(state), 1u);
     __syncthreads();
-    for (int base = 0; base < nparts; base += kScanThreads) {
-        const int i = base + threadIdx.x;
-        const uint32_t v = i < nparts ? parts[i] : 0u;
-        const uint32_t ex = block_exclusive(v, &total);
-        const uint32_t carry = carry_s;
-        if (i < nparts) parts[i] = carry + ex;
-        __syncthreads();
-        if (threadIdx.x == 0) carry_s = carry + total;
-        __syncthreads();
-    }
-}
-
-__global__ void __launch_bounds__(kScanThreads) k_scan_down(uint32_t* __restrict__ counts, int ncells,
-                                                            const uint32_t* __restrict__ parts,
-                                                            uint32_t* __restrict__ cstart) {
-    const int base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
+    const int tile = (int)s_tile;
+    if (tile == 0 && threadIdx.x == 0 && zero_word) *zero_word = 0u;  // the step's deferred-target count
+    unsigned long long* flags = state + 1;
+    const int base = tile * kScanTile + threadIdx.x * kScanItems;
     uint32_t v[kScanItems];
-    uint32_t s = 0;
+    if (base + kScanItems <= ncells) {
+        const uint4 q = *reinterpret_cast<const uint4*>(counts + base);
+        v[0] = q.x;
+        v[1] = q.y;
+        v[2] = q.z;
+        v[3] = q.w;
+    } else {
 #pragma unroll
-    for (int k = 0; k < kScanItems; ++k) {
-        v[k] = base + k < ncells ? counts[base + k] : 0u;
-        s += v[k];
+        for (int k = 0; k < kScanItems; ++k) v[k] = base + k < ncells ? counts[base + k] : 0u;
     }
-    __shared__ uint32_t total;
-    uint32_t run = block_exclusive(s, &total) + parts[blockIdx.x];
+    uint32_t sum = 0;
 #pragma unroll
-    for (int k = 0; k < kScanItems; ++k) {
-        const int c = base + k;
-        if (c < ncells) {
-            cstart[c] = run;
-            counts[c] = 0;  // ready for the next counting pass
-            if (c == ncells - 1) cstart[ncells] = run + v[k];
+    for (int k = 0; k < kScanItems; ++k) sum += v[k];
+    const uint32_t ex = block_exclusive(sum, &total);
+    if (threadIdx.x < 32) {
+        // Warp-parallel look-back: lanes read the status words of the 32
+        // nearest earlier tiles; the sums of tiles up to the nearest one with
+        // a published inclusive prefix (tile -1 counts as inclusive 0) are
+        // added, otherwise the window moves 32 tiles back.
+        const int lane = threadIdx.x;
+        uint32_t excl = 0;
+        if (tile == 0) {
+            if (lane == 0) atomicExch(flags, kTileInclusive | total);
+        } else {
+            if (lane == 0) atomicExch(flags + tile, kTileAggregate | total);
+            for (int p = tile - 1;; p -= 32) {
+                const int idx = p - lane;
+                unsigned long long f = idx >= 0 ? load_volatile(flags + idx) : kTileInclusive;
+                int spins = 0;
+                while ((f >> 32) == 0ull) {
+                    if (++spins > kLookbackSpinLimit) {
+                        atomicOr(status, kDevSpinLimit);
+                        f = kTileInclusive;
+                        break;
+                    }
+                    __nanosleep(64);
+                    f = load_volatile(flags + idx);
+                }
+                const unsigned inc = __ballot_sync(kFull, (f >> 32) == 2ull);
+                const int last = inc ? __ffs(inc) - 1 : 31;
+                uint32_t v = lane <= last ? (uint32_t)f : 0u;
+#pragma unroll
+                for (int d = 16; d > 0; d >>= 1) v += __shfl_xor_sync(kFull, v, d);
+                excl += v;
+                if (inc) break;
+            }
+            if (lane == 0) atomicExch(flags + tile, kTileInclusive | (excl + total));
         }
-        run += v[k];
+        if (lane == 0) s_prefix = excl;
+    }
+    __syncthreads();
+    uint32_t run = s_prefix + ex;
+    if (base + kScanItems <= ncells) {
+        uint4 o;
+        o.x = run;
+        o.y = run + v[0];
+        o.z = o.y + v[1];
+        o.w = o.z + v[2];
+        *reinterpret_cast<uint4*>(cstart + base) = o;
+        *reinterpret_cast<uint4*>(counts + base) = make_uint4(0u, 0u, 0u, 0u);
+        if (base + kScanItems == ncells) cstart[ncells] = o.w + v[3];
+    } else {
+#pragma unroll
+        for (int k = 0; k < kScanItems; ++k) {
+            const int c = base + k;
+            if (c < ncells) {
+                cstart[c] = run;
+                counts[c] = 0;
+                if (c == ncells - 1) cstart[ncells] = run + v[k];
+            }
+            run += v[k];
+        }
     }
 }
 
@@ -235,22 +278,39 @@ __global__ void __launch_bounds__(kThreads) k_scatter(int n, const uint32_t* __r
     perm[cstart[cell[i]] + rank[i]] = (uint32_t)i;
 }
 
+// Orders x for the in-cell sort: NaN after every number, so that the order
+// is total and agrees with float comparison on the numbers.
+__device__ __forceinline__ float sort_x(float x) { return isnan(x) ? INFINITY : x; }
+
+// Places particle i = perm[s] within its cell.  Two ranks among the cell's
+// members: by index (the reference's stable order, Physics.java:342-348) and
+// by (x, index).  B holds each cell in x order, so that a target's candidate
+// runs are sorted by x; refslot maps a B slot to its slot in the reference
+// order, where the force kernel writes the particle's next state.
 template <int D>
 __global__ void __launch_bounds__(kThreads) k_gather(int n, const uint32_t* __restrict__ perm,
                                                      const uint32_t* __restrict__ cell,
                                                      const uint32_t* __restrict__ cstart, StateBuf<D> a,
-                                                     StateBuf<D> b, int32_t* __restrict__ cell_sorted) {
+                                                     StateBuf<D> b, uint32_t* __restrict__ refslot,
+                                                     int32_t* __restrict__ cell_sorted) {
     const int s = blockIdx.x * kThreads + threadIdx.x;
     if (s >= n) return;
     const uint32_t i = perm[s];
     const uint32_t c = cell[i];
     const uint32_t st = cstart[c], en = cstart[c + 1];
-    uint32_t r = 0;
-    for (uint32_t t = st; t < en; ++t) r += __ldg(perm + t) < i ? 1u : 0u;
-    const uint32_t d = st + r;
-    b.pt[d] = a.pt[i];
-    b.vel[d] = a.vel[i];
-    if (cell_sorted) cell_sorted[d] = (int32_t)c;
+    const float4 me = a.pt[i];
+    const float xi = sort_x(me.x);
+    uint32_t ri = 0, rx = 0;
+    for (uint32_t t = st; t < en; ++t) {
+        const uint32_t j = __ldg(perm + t);
+        const float xj = sort_x(__ldg(&a.pt[j].x));
+        ri += j < i ? 1u : 0u;
+        rx += (xj < xi || (xj == xi && j < i)) ? 1u : 0u;
+    }
+    b.pt[st + rx] = me;
+    b.vel[st + rx] = a.vel[i];
+    refslot[st + rx] = st + ri;
+    if (cell_sorted) cell_sorted[st + ri] = (int32_t)c;
 }
 
 }  // namespace
@@ -277,16 +337,9 @@ void launch_download(cudaStream_t st, int n, StateBuf<D> a, double* pos, double*
 
 int scan_blocks(int ncells) { return blocks_for(ncells, kScanTile); }
 
-void launch_scan_reduce(cudaStream_t st, const uint32_t* counts, int ncells, uint32_t* parts) {
-    k_scan_reduce<<<scan_blocks(ncells), kScanThreads, 0, st>>>(counts, ncells, parts);
-}
-
-void launch_scan_parts(cudaStream_t st, uint32_t* parts, int nparts) {
-    k_scan_parts<<<1, kScanThreads, 0, st>>>(parts, nparts);
-}
-
-void launch_scan_down(cudaStream_t st, uint32_t* counts, int ncells, const uint32_t* parts, uint32_t* cstart) {
-    k_scan_down<<<scan_blocks(ncells), kScanThreads, 0, st>>>(counts, ncells, parts, cstart);
+void launch_scan(cudaStream_t st, uint32_t* counts, int ncells, uint32_t* cstart, unsigned long long* state,
+                 uint32_t* status, uint32_t* zero_word) {
+    k_scan<<<scan_blocks(ncells), kScanThreads, 0, st>>>(counts, ncells, cstart, state, status, zero_word);
 }
 
 void launch_scatter(cudaStream_t st, int n, const uint32_t* cell, const uint32_t* rank, const uint32_t* cstart,
@@ -297,9 +350,9 @@ void launch_scatter(cudaStream_t st, int n, const uint32_t* cell, const uint32_t
 
 template <int D>
 void launch_gather(cudaStream_t st, int n, const uint32_t* perm, const uint32_t* cell, const uint32_t* cstart,
-                   StateBuf<D> a, StateBuf<D> b, int32_t* cell_sorted) {
+                   StateBuf<D> a, StateBuf<D> b, uint32_t* refslot, int32_t* cell_sorted) {
     if (n <= 0) return;
-    k_gather<D><<<blocks_for(n, kThreads), kThreads, 0, st>>>(n, perm, cell, cstart, a, b, cell_sorted);
+    k_gather<D><<<blocks_for(n, kThreads), kThreads, 0, st>>>(n, perm, cell, cstart, a, b, refslot, cell_sorted);
 }
 
 template void launch_upload<2>(cudaStream_t, int, const double*, const double*, const int32_t*, int, StateBuf<2>,
@@ -311,8 +364,8 @@ template void launch_rebin<3>(cudaStream_t, int, StateBuf<3>, uint32_t*, uint32_
 template void launch_download<2>(cudaStream_t, int, StateBuf<2>, double*, double*, int32_t*, int32_t*);
 template void launch_download<3>(cudaStream_t, int, StateBuf<3>, double*, double*, int32_t*, int32_t*);
 template void launch_gather<2>(cudaStream_t, int, const uint32_t*, const uint32_t*, const uint32_t*, StateBuf<2>,
-                               StateBuf<2>, int32_t*);
+                               StateBuf<2>, uint32_t*, int32_t*);
 template void launch_gather<3>(cudaStream_t, int, const uint32_t*, const uint32_t*, const uint32_t*, StateBuf<3>,
-                               StateBuf<3>, int32_t*);
+                               StateBuf<3>, uint32_t*, int32_t*);
 
 }  // namespace plg

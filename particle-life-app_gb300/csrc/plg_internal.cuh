@@ -111,8 +111,12 @@ struct ForceParams {
     int slmask_ok;          // nx >= 4: sliver targets need the stencil correction
     const float* matrix;    // ntypes x ntypes, row-major, FP32
     float lo, hi, tiny;     // FP32 d2 decision band around rmax^2
+    float xwin;             // > sqrt(hi) with margin: |dx| bound of any pair with d2 < hi
     float inv_rmax;
     float beta, inv_beta, one_plus_beta, inv_one_minus_beta;
+    float m2_inv_rmax;      // -2 / rmax
+    float beta_rmax;        // beta * rmax: below this distance the linear repulsion applies
+    float k1;               // 1 / (beta * rmax): (|d|/(beta rmax) - 1) / |d| = k1 - 1/|d|
     float ff;               // (float) pow(friction, 60 dt)
     float scale;            // (float) (rmax * force * dt)
     float dt;
@@ -150,19 +154,28 @@ void launch_download(cudaStream_t st, int n, StateBuf<D> a, double* pos, double*
                      int32_t* id);
 
 int scan_blocks(int ncells);
-void launch_scan_reduce(cudaStream_t st, const uint32_t* counts, int ncells, uint32_t* parts);
-void launch_scan_parts(cudaStream_t st, uint32_t* parts, int nparts);
-void launch_scan_down(cudaStream_t st, uint32_t* counts, int ncells, const uint32_t* parts, uint32_t* cstart);
+// state: (scan_blocks + 1) words, zeroed before each launch; *zero_word is
+// set to 0 (the step's deferred-target count) when not null.
+void launch_scan(cudaStream_t st, uint32_t* counts, int ncells, uint32_t* cstart, unsigned long long* state,
+                 uint32_t* status, uint32_t* zero_word);
 void launch_scatter(cudaStream_t st, int n, const uint32_t* cell, const uint32_t* rank, const uint32_t* cstart,
                     uint32_t* perm);
 
 template <int D>
 void launch_gather(cudaStream_t st, int n, const uint32_t* perm, const uint32_t* cell, const uint32_t* cstart,
-                   StateBuf<D> a, StateBuf<D> b, int32_t* cell_sorted);
+                   StateBuf<D> a, StateBuf<D> b, uint32_t* refslot, int32_t* cell_sorted);
 
+// `defer`: 1 + n words, word 0 zeroed before the step (deferred-target list).
 template <int D>
 void launch_force(cudaStream_t st, const ForceParams& p, bool general, StateBuf<D> b, const uint32_t* cstart,
-                  StateBuf<D> a, uint32_t* cell, uint32_t* rank, uint32_t* counts, const DebugOut* dbg);
+                  StateBuf<D> a, uint32_t* cell, uint32_t* rank, uint32_t* counts, uint32_t* defer,
+                  const uint32_t* refslot, const DebugOut* dbg);
+
+// Completes the targets k_force_tile deferred (no-op for nx < 3).
+template <int D>
+void launch_force_fixup(cudaStream_t st, const ForceParams& p, bool general, StateBuf<D> b, const uint32_t* cstart,
+                        StateBuf<D> a, uint32_t* cell, uint32_t* rank, uint32_t* counts, uint32_t* defer,
+                        const uint32_t* refslot, const DebugOut* dbg, int blocks);
 
 cudaError_t probe_fp32_peak(double* tflops);
 

@@ -5,6 +5,7 @@
 // one step.  See plg_internal.cuh for the device data layout.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <atomic>
 #include <chrono>
 #include <climits>
@@ -30,7 +31,7 @@ constexpr int kMaxAxisCells = 1 << 20;
 constexpr int kMaxTypes = 1024;
 constexpr double kBandRel = 1.0 / (1 << 19);  // FP32 decision band: 2^-19 relative
 
-const char* kKernelNames[PLG_K_COUNT] = {"scan_reduce", "scan_parts", "scan_down", "scatter", "gather", "force"};
+const char* kKernelNames[PLG_K_COUNT] = {"scan", "scatter", "gather", "force", "fixup"};
 
 // Staging layout for host <-> device copies: pos[3n] vel[3n] (double), type[n] id[n] (int32).
 size_t stage_bytes(int64_t cap) { return (size_t)cap * (3 * 8 + 3 * 8 + 4 + 4); }
@@ -61,8 +62,8 @@ struct plg_ctx {
     uint32_t* cstart = nullptr;
     int64_t cells_cap = 0;
     int64_t cstart_cap = 0;
-    uint32_t* parts = nullptr;
-    int64_t parts_cap = 0;
+    unsigned long long* scan_state = nullptr;  // tile counter + look-back status words
+    int64_t scan_cap = 0;
 
     // matrix
     int ntypes = 0;
@@ -77,6 +78,9 @@ struct plg_ctx {
     uint32_t* cell = nullptr;
     uint32_t* rank = nullptr;
     uint32_t* perm = nullptr;
+    uint32_t* defer = nullptr;  // deferred-target count + list (force -> fixup)
+    uint32_t* refslot = nullptr;  // B slot -> slot of the reference order
+    int fixup_blocks = 0;
     unsigned char* stage = nullptr;
 
     uint32_t* status_d = nullptr;
@@ -210,12 +214,18 @@ void compute_force_params(plg_ctx* c) {
     if ((double)hi < hi_d) hi = std::nextafter(hi, INFINITY);
     p.lo = lo;
     p.hi = hi;
+    // Every pair with FP32 d2 < hi has |dx| < sqrt(hi) (1 + 2^-24); the margin
+    // also covers the rounding of pxe +- xwin for coordinates in [-1, 1].
+    p.xwin = (float)(std::sqrt((double)hi) * (1.0 + std::ldexp(1.0, -10)) + std::ldexp(1.0, -22));
     p.tiny = std::ldexp(1.0f, -100);
     p.inv_rmax = (float)(1.0 / s.rmax);
     p.beta = (float)s.beta;
     p.inv_beta = (float)(1.0 / s.beta);
     p.one_plus_beta = (float)(1.0 + s.beta);
     p.inv_one_minus_beta = (float)(1.0 / (1.0 - s.beta));
+    p.m2_inv_rmax = (float)(-2.0 / s.rmax);
+    p.beta_rmax = (float)(s.beta * s.rmax);
+    p.k1 = (float)(1.0 / (s.beta * s.rmax));
     p.ff = (float)std::pow(s.friction, 60 * s.dt);
     p.scale = (float)(s.rmax * s.force * s.dt);
     p.dt = (float)s.dt;
@@ -238,24 +248,24 @@ void enqueue_body(plg_ctx* c, const DebugOut* dbg, int32_t* cell_sorted) {
     auto k1 = [&](int k) {
         if (c->profiling) cudaEventRecord(c->pev[k][1], st);
     };
-    k0(PLG_K_SCAN_REDUCE);
-    launch_scan_reduce(st, c->counts, c->ncells, c->parts);
-    k1(PLG_K_SCAN_REDUCE);
-    k0(PLG_K_SCAN_PARTS);
-    launch_scan_parts(st, c->parts, c->nparts);
-    k1(PLG_K_SCAN_PARTS);
-    k0(PLG_K_SCAN_DOWN);
-    launch_scan_down(st, c->counts, c->ncells, c->parts, c->cstart);
-    k1(PLG_K_SCAN_DOWN);
+    k0(PLG_K_SCAN);
+    cudaMemsetAsync(c->scan_state, 0, sizeof(unsigned long long) * (size_t)(c->nparts + 1), st);
+    launch_scan(st, c->counts, c->ncells, c->cstart, c->scan_state, c->status_d, c->general ? nullptr : c->defer);
+    k1(PLG_K_SCAN);
     k0(PLG_K_SCATTER);
     launch_scatter(st, n, c->cell, c->rank, c->cstart, c->perm);
     k1(PLG_K_SCATTER);
     k0(PLG_K_GATHER);
-    launch_gather<D>(st, n, c->perm, c->cell, c->cstart, buf_a<D>(c), buf_b<D>(c), cell_sorted);
+    launch_gather<D>(st, n, c->perm, c->cell, c->cstart, buf_a<D>(c), buf_b<D>(c), c->refslot, cell_sorted);
     k1(PLG_K_GATHER);
     k0(PLG_K_FORCE);
-    launch_force<D>(st, c->fp, c->general, buf_b<D>(c), c->cstart, buf_a<D>(c), c->cell, c->rank, c->counts, dbg);
+    launch_force<D>(st, c->fp, c->general, buf_b<D>(c), c->cstart, buf_a<D>(c), c->cell, c->rank, c->counts,
+                    c->defer, c->refslot, dbg);
     k1(PLG_K_FORCE);
+    k0(PLG_K_FIXUP);
+    launch_force_fixup<D>(st, c->fp, c->general, buf_b<D>(c), c->cstart, buf_a<D>(c), c->cell, c->rank, c->counts,
+                          c->defer, c->refslot, dbg, c->fixup_blocks);
+    k1(PLG_K_FIXUP);
 }
 
 void enqueue_body_dim(plg_ctx* c, const DebugOut* dbg, int32_t* cell_sorted) {
@@ -278,7 +288,7 @@ int enqueue_rebin(plg_ctx* c) {
 }
 
 int accumulate_profile(plg_ctx* c) {
-    CK(c, cudaEventSynchronize(c->pev[PLG_K_FORCE][1]));
+    CK(c, cudaEventSynchronize(c->pev[PLG_K_COUNT - 1][1]));  // the step's last kernel
     for (int k = 0; k < PLG_K_COUNT; ++k) {
         float ms = 0.f;
         CK(c, cudaEventElapsedTime(&ms, c->pev[k][0], c->pev[k][1]));
@@ -362,8 +372,8 @@ int read_status(plg_ctx* c) {
 
 int free_all(plg_ctx* c) {
     destroy_graph(c);
-    void* ptrs[] = {c->bounds, c->counts, c->cstart, c->parts, c->matrix, c->apt, c->bpt, c->avel, c->bvel,
-                    c->cell, c->rank, c->perm, c->stage, c->status_d, c->dbg_pairs, c->dbg_hsum, c->dbg_hxor,
+    void* ptrs[] = {c->bounds, c->counts, c->cstart, c->scan_state, c->matrix, c->apt, c->bpt, c->avel, c->bvel,
+                    c->cell, c->rank, c->perm, c->defer, c->refslot, c->stage, c->status_d, c->dbg_pairs, c->dbg_hsum, c->dbg_hxor,
                     c->dbg_cand, c->dbg_acc, c->dbg_cell};
     for (void* p : ptrs)
         if (p) cudaFree(p);
@@ -456,6 +466,11 @@ int plg_create(int dim, int64_t capacity, plg_ctx** out) {
     const size_t cap = (size_t)capacity;
     e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) rc = PLG_E_CUDA;
+    int sms = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device) != cudaSuccess) rc = PLG_E_CUDA;
+    // Deferred targets are rare (FP64 band pairs, overfull segments): one
+    // wave of 256-thread blocks, capped by the capacity.
+    c->fixup_blocks = (int)std::min<int64_t>(2 * (int64_t)sms, (capacity + 255) / 256);
     dmalloc((void**)&c->apt, sizeof(float4) * cap);
     dmalloc((void**)&c->bpt, sizeof(float4) * cap);
     dmalloc(&c->avel, vel_sz * cap);
@@ -463,6 +478,8 @@ int plg_create(int dim, int64_t capacity, plg_ctx** out) {
     dmalloc((void**)&c->cell, sizeof(uint32_t) * cap);
     dmalloc((void**)&c->rank, sizeof(uint32_t) * cap);
     dmalloc((void**)&c->perm, sizeof(uint32_t) * cap);
+    dmalloc((void**)&c->defer, sizeof(uint32_t) * (cap + 1));
+    dmalloc((void**)&c->refslot, sizeof(uint32_t) * cap);
     dmalloc((void**)&c->stage, stage_bytes(capacity));
     dmalloc((void**)&c->status_d, 64);
     if (!rc && cudaMallocHost((void**)&c->status_h, 64) != cudaSuccess) rc = PLG_E_NO_MEMORY;
@@ -506,7 +523,7 @@ int plg_set_settings(plg_ctx* c, const plg_settings* s) {
         if ((rc = grow(c, &c->counts, &c->cells_cap, cells, "counts"))) return rc;
         if ((rc = grow(c, &c->cstart, &c->cstart_cap, cells + 1, "cstart"))) return rc;
         const int nparts = scan_blocks((int)cells);
-        if ((rc = grow(c, &c->parts, &c->parts_cap, nparts, "parts"))) return rc;
+        if ((rc = grow(c, &c->scan_state, &c->scan_cap, (int64_t)nparts + 1, "scan state"))) return rc;
         c->nx = nx;
         c->ncells = (int)cells;
         c->nparts = nparts;
@@ -760,6 +777,19 @@ int plg_debug_step(plg_ctx* c, int32_t* cell, int32_t* pairs, uint64_t* hash_sum
     CK(c, cudaStreamSynchronize(st));
     if (candidates) *candidates = (int64_t)cand;
     return read_status(c);
+}
+
+int plg_step_stats(plg_ctx* c, int64_t* deferred) {
+    if (!c || !deferred) return PLG_E_INVALID_ARG;
+    DeviceGuard g(c->device);
+    uint32_t v = 0;
+    if (!c->general && c->defer) {
+        CK(c, cudaMemcpyAsync(c->status_h + 1, c->defer, sizeof(uint32_t), cudaMemcpyDeviceToHost, c->stream));
+        CK(c, cudaStreamSynchronize(c->stream));
+        v = c->status_h[1];
+    }
+    *deferred = v;
+    return PLG_OK;
 }
 
 int plg_probe_fp32_peak(double* tflops) {

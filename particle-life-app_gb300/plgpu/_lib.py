@@ -26,7 +26,7 @@ PLG_E_CAPACITY = 9
 
 PLG_ACCEL_PARTICLE_LIFE = 1
 
-KERNELS = ["scan_reduce", "scan_parts", "scan_down", "scatter", "gather", "force"]
+KERNELS = ["scan", "scatter", "gather", "force", "fixup"]
 
 
 class plg_settings(C.Structure):
@@ -82,6 +82,7 @@ SIGNATURES = {
     "plg_kernel_name": (C.c_char_p, [C.c_int32]),
     "plg_debug_step": (C.c_int, [_P, _I32P, _I32P, _U64P, _U64P, _FP, _I64P]),
     "plg_probe_fp32_peak": (C.c_int, [_DP]),
+    "plg_step_stats": (C.c_int, [_P, _I64P]),
 }
 
 _lib = None

@@ -4,10 +4,16 @@ Bit-exact: the sorted order (particle ids after the step), the cell of every
 particle, and each particle's interacting-pair set (count, sum and xor of
 splitmix64(id)).  Floating point, on the same FP32 start state:
   - accelerations (sum of Accelerator.accelerate terms): norm-wise relative
-    error <= 1e-5, and per particle |a - a*| / sum_j |term_j| <= 1e-5;
+    error <= 1e-5, and per particle |a - a*| / sum_j max(1, |a_ij|) <= 1e-5
+    (each term is f(r) r/|r| with |f| <= max(1, |a_ij|); f vanishes at
+    r = beta and r = 1, so |term_j| itself is no error scale);
   - velocities after the step: norm-wise relative error <= 1e-5;
-  - positions after the step: max periodic distance <= 2e-7 (FP32 rounding of
-    a coordinate in [0,1) is <= 6e-8).
+  - positions after the step, per coordinate: periodic distance
+    <= 1.2e-7 + dt (1e-5 |v| + 1e-5 rmax force dt sum_j max(1, |a_ij|)):
+    FP32 rounding of a coordinate in [0,1) (<= 6e-8) plus dt times the
+    velocity error the two tolerances above allow.
+The norm-wise acceleration check is skipped for worlds whose every pair sits
+at a zero of the force (the exact-rmax lattice), where it is ill-conditioned.
 """
 import numpy as np
 import pytest
@@ -19,10 +25,10 @@ pytestmark = pytest.mark.gpu
 
 ACC_TOL = 1e-5
 VEL_TOL = 1e-5
-POS_TOL = 2e-7
+POS_ABS = 1.2e-7
 
 
-def check_step(spec: WorldSpec, gpu, exact_only=False):
+def check_step(spec: WorldSpec, gpu, exact_only=False, normwise=True):
     g, (gpos, gvel, gtypes, gids) = run_gpu_debug(spec)
     d, o = run_oracle_debug(spec)
     assert np.array_equal(gids, o.ids), "sorted order (ids) differs from the oracle"
@@ -36,14 +42,18 @@ def check_step(spec: WorldSpec, gpu, exact_only=False):
         return out
     acc_g = g["acc"].astype(np.float64)
     e = accel_errors(acc_g, d["acc"])
-    assert e["normwise"] <= ACC_TOL, e
-    scale = np.where(d["accabs"] > 0, d["accabs"], 1.0)
+    if normwise:
+        assert e["normwise"] <= ACC_TOL, e
+    scale = np.where(d["fscale"] > 0, d["fscale"], 1.0)
     per = np.linalg.norm(acc_g - d["acc"], axis=1) / scale
     assert per.max() <= ACC_TOL, per.max()
     dim = spec.dim
-    assert norm_rel(gvel[:, :dim], o.vel[:, :dim]) <= VEL_TOL
-    dp = min_image(gpos[:, :dim] - o.pos[:, :dim], spec.wrap)
-    assert np.abs(dp).max() <= POS_TOL, np.abs(dp).max()
+    if normwise:
+        assert norm_rel(gvel[:, :dim], o.vel[:, :dim]) <= VEL_TOL
+    dp = np.abs(min_image(gpos[:, :dim] - o.pos[:, :dim], spec.wrap))
+    dv = VEL_TOL * np.abs(o.vel[:, :dim]) + ACC_TOL * (spec.rmax * spec.force * spec.dt) * d["fscale"][:, None]
+    bound = POS_ABS + spec.dt * dv
+    assert np.all(dp <= bound), float((dp / bound).max())
     out.update(e)
     return out
 
@@ -113,10 +123,10 @@ def test_2d_lattice_at_exactly_rmax(gpu):
     rng = np.random.Generator(np.random.Philox(8))
     spec = WorldSpec(2, pos, np.zeros((n, 3)), rng.integers(0, 3, n).astype(np.int32),
                      f32(2 * rng.random((3, 3)) - 1), rmax)
-    r = check_step(spec, gpu)
+    r = check_step(spec, gpu, normwise=False)
     assert r["pairs"] == 4.0
-    spec.pos[:, 0] = np.nextafter(spec.pos[:, 0].astype(np.float32) * np.float32(1.0), np.float32(2)).astype(np.float64)
-    check_step(spec, gpu)
+    spec.pos[:, 0] = np.nextafter(spec.pos[:, 0].astype(np.float32), np.float32(2)).astype(np.float64)
+    check_step(spec, gpu, normwise=False)
 
 
 def test_2d_coincident_particles(gpu):
@@ -131,6 +141,14 @@ def test_2d_fast_particles_wrap_many_times(gpu):
     rng = np.random.Generator(np.random.Philox(10))
     spec.vel[:, :2] = f32(rng.uniform(-400, 400, (spec.n, 2)))
     check_step(spec, gpu)
+
+
+def test_2d_dense_clusters_overflow_shared_memory(gpu):
+    """Clusters far denser than shared memory can stage: those targets take
+    the deferred (global-memory) path."""
+    spec = blob_world(60_000, 5, 0.01, nblobs=12, sigma=0.004, seed=14, dim=2)
+    r = check_step(spec, gpu)
+    assert r["pairs"] > 100
 
 
 def test_3d_uniform(gpu):
