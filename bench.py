@@ -257,15 +257,20 @@ def run_ours(args):
     P, I = _lib.C.c_double, _lib.C.c_int32
     check(lib.plg_download(w.ctx, _lib.ptr(hp, P), _lib.ptr(hv, P), _lib.ptr(ht, I), _lib.ptr(hi, I)), w.ctx, "dl")
     e2e_s = 0.0
+    parts = np.zeros(3)
     barrier()
     for k in range(args.e2e_steps):
         flush_l2()
         t0 = time.perf_counter()
         check(lib.plg_upload(w.ctx, n, _lib.ptr(hp, P), _lib.ptr(hv, P), _lib.ptr(ht, I)), w.ctx, "plg_upload")
+        t1 = time.perf_counter()
         check(lib.plg_step(w.ctx, 1), w.ctx, "plg_step")
+        t2 = time.perf_counter()
         check(lib.plg_download(w.ctx, _lib.ptr(hp, P), _lib.ptr(hv, P), _lib.ptr(ht, I), _lib.ptr(hi, I)), w.ctx,
               "plg_download")
-        e2e_s += time.perf_counter() - t0
+        t3 = time.perf_counter()
+        e2e_s += t3 - t0
+        parts += (t1 - t0, t2 - t1, t3 - t2)
     barrier()
     clk = clocks.stop()
     if dist is not None:
@@ -274,6 +279,7 @@ def run_ours(args):
         e2e_s = float(t.item())
     e2e_value = world_size * n * args.e2e_steps / e2e_s
 
+    deferred = w.deferred()
     # pair statistics of the current state (one instrumented step)
     dbg = w.debug_step()
     cand = dbg["candidates"] / n
@@ -328,7 +334,9 @@ def run_ours(args):
                        "l2": "warm (not flushed)" if args.no_flush else "flushed (256 MB write) between steps"},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": n * (24 + 24 + 4),
                     "d2h_bytes_per_step": n * (24 + 24 + 4 + 4), "steps": args.e2e_steps,
-                    "api": "plg_upload + plg_step + plg_download, pinned host buffers, host wall clock"},
+                    "api": "plg_upload + plg_step + plg_download, pinned host buffers, host wall clock",
+                    "ms_upload_step_download": [round(1e3 * x / args.e2e_steps, 4) for x in parts]},
+            "deferred_targets_last_step": deferred,
             "gpu_launches": len(_lib.KERNELS) * args.steps,
             "roofline": roofline,
             "kernels": kern,

@@ -7,16 +7,12 @@
 //   scan      counts -> exclusive offsets (Physics.java:334-340), single
 //             pass with decoupled look-back; counts reset
 //   scatter   perm[cstart[cell]+rank] = i (unstable: atomics order warps)
-//   gather    rank_stable(i) = #{members of i's cell with a smaller index},
-//             rank_x(i) = #{members before i in (x, index) order};
-//             B[cstart[cell] + rank_x] = A[i],
-//             refslot[cstart[cell] + rank_x] = cstart[cell] + rank_stable
-// The stable rank reproduces the order of the reference's sequential
-// scatter (Physics.java:342-348): the force kernel writes each particle's
-// next state to A[refslot[slot]], so A always holds the reference's order.
-// The x order inside B lets the force kernel cut each candidate run to the
-// |dx| <= rmax window.  The re-ranks cost sum_c n_c^2 compares, a ninth of
-// the force loop's sum_c n_c * (9 neighbour cells) candidate tests.
+//   gather    rank_stable(i) = #{members of i's cell with a smaller index};
+//             B[cstart[cell] + rank_stable] = A[i]
+// The gather makes the sort stable, so the cell-sorted order equals the one
+// the reference's sequential scatter (Physics.java:342-348) produces.  The
+// stable re-rank costs sum_c n_c^2 compares, a ninth of the force loop's
+// sum_c n_c * (9 neighbour cells) candidate tests.
 #include "plg_internal.cuh"
 
 namespace plg {
@@ -278,39 +274,24 @@ __global__ void __launch_bounds__(kThreads) k_scatter(int n, const uint32_t* __r
     perm[cstart[cell[i]] + rank[i]] = (uint32_t)i;
 }
 
-// Orders x for the in-cell sort: NaN after every number, so that the order
-// is total and agrees with float comparison on the numbers.
-__device__ __forceinline__ float sort_x(float x) { return isnan(x) ? INFINITY : x; }
-
-// Places particle i = perm[s] within its cell.  Two ranks among the cell's
-// members: by index (the reference's stable order, Physics.java:342-348) and
-// by (x, index).  B holds each cell in x order, so that a target's candidate
-// runs are sorted by x; refslot maps a B slot to its slot in the reference
-// order, where the force kernel writes the particle's next state.
+// Places particle i = perm[s] at its rank among its cell's members by
+// index: the order of the reference's sequential scatter
+// (Physics.java:342-348).
 template <int D>
 __global__ void __launch_bounds__(kThreads) k_gather(int n, const uint32_t* __restrict__ perm,
                                                      const uint32_t* __restrict__ cell,
                                                      const uint32_t* __restrict__ cstart, StateBuf<D> a,
-                                                     StateBuf<D> b, uint32_t* __restrict__ refslot,
-                                                     int32_t* __restrict__ cell_sorted) {
+                                                     StateBuf<D> b, int32_t* __restrict__ cell_sorted) {
     const int s = blockIdx.x * kThreads + threadIdx.x;
     if (s >= n) return;
     const uint32_t i = perm[s];
     const uint32_t c = cell[i];
     const uint32_t st = cstart[c], en = cstart[c + 1];
-    const float4 me = a.pt[i];
-    const float xi = sort_x(me.x);
-    uint32_t ri = 0, rx = 0;
-    for (uint32_t t = st; t < en; ++t) {
-        const uint32_t j = __ldg(perm + t);
-        const float xj = sort_x(__ldg(&a.pt[j].x));
-        ri += j < i ? 1u : 0u;
-        rx += (xj < xi || (xj == xi && j < i)) ? 1u : 0u;
-    }
-    b.pt[st + rx] = me;
-    b.vel[st + rx] = a.vel[i];
-    refslot[st + rx] = st + ri;
-    if (cell_sorted) cell_sorted[st + ri] = (int32_t)c;
+    uint32_t r = 0;
+    for (uint32_t t = st; t < en; ++t) r += __ldg(perm + t) < i ? 1u : 0u;
+    b.pt[st + r] = a.pt[i];
+    b.vel[st + r] = a.vel[i];
+    if (cell_sorted) cell_sorted[st + r] = (int32_t)c;
 }
 
 }  // namespace
@@ -350,9 +331,9 @@ void launch_scatter(cudaStream_t st, int n, const uint32_t* cell, const uint32_t
 
 template <int D>
 void launch_gather(cudaStream_t st, int n, const uint32_t* perm, const uint32_t* cell, const uint32_t* cstart,
-                   StateBuf<D> a, StateBuf<D> b, uint32_t* refslot, int32_t* cell_sorted) {
+                   StateBuf<D> a, StateBuf<D> b, int32_t* cell_sorted) {
     if (n <= 0) return;
-    k_gather<D><<<blocks_for(n, kThreads), kThreads, 0, st>>>(n, perm, cell, cstart, a, b, refslot, cell_sorted);
+    k_gather<D><<<blocks_for(n, kThreads), kThreads, 0, st>>>(n, perm, cell, cstart, a, b, cell_sorted);
 }
 
 template void launch_upload<2>(cudaStream_t, int, const double*, const double*, const int32_t*, int, StateBuf<2>,
@@ -364,8 +345,8 @@ template void launch_rebin<3>(cudaStream_t, int, StateBuf<3>, uint32_t*, uint32_
 template void launch_download<2>(cudaStream_t, int, StateBuf<2>, double*, double*, int32_t*, int32_t*);
 template void launch_download<3>(cudaStream_t, int, StateBuf<3>, double*, double*, int32_t*, int32_t*);
 template void launch_gather<2>(cudaStream_t, int, const uint32_t*, const uint32_t*, const uint32_t*, StateBuf<2>,
-                               StateBuf<2>, uint32_t*, int32_t*);
+                               StateBuf<2>, int32_t*);
 template void launch_gather<3>(cudaStream_t, int, const uint32_t*, const uint32_t*, const uint32_t*, StateBuf<3>,
-                               StateBuf<3>, uint32_t*, int32_t*);
+                               StateBuf<3>, int32_t*);
 
 }  // namespace plg

@@ -8,14 +8,16 @@
 // and, in its epilogue, the counting pass of the next makeContainers
 // (Physics.java:328-332) on the new position.
 //
-// Tiling.  A block takes 128 consecutive targets of the sorted order.  Their
-// cells are nondecreasing, so they fall into a few "segments" (targets of one
-// grid row: one y in 2D, one (y, z) in 3D).  For each segment the block stages
-// into shared memory, with coalesced loads, the 3 (3D: 9) stencil rows over
-// the segment's columns plus one halo column each side; every target then
-// reads its 3 (9) candidate runs as contiguous shared-memory ranges.  A
-// segment whose stencil does not fit falls back to reading the runs from
-// global memory (stencil_scan).
+// Tiling.  A block takes 128 consecutive targets of the sorted order, one
+// thread each.  Their cells are nondecreasing, so they fall into a few
+// "segments" (targets of one grid row: one y in 2D, one (y, z) in 3D).  For
+// each segment the block stages into shared memory, with coalesced loads, the
+// segment's stencil (3 rows in 2D, 9 in 3D, over the segment's columns plus a
+// halo column each side) column by column, so that the whole neighbourhood of
+// a target in column cx is one contiguous run (columns cx-1..cx+1).  The
+// candidate loop is branch-free FP32.  A target that meets a candidate needing
+// the FP64 decision, or whose segment does not fit in shared memory, is
+// deferred to k_force_fixup (one warp per target, global-memory stencil).
 //
 // Pair test.  The reference keeps a pair when d2 != 0 && d2 <= rmax*rmax in
 // FP64, with d = wrapConnection(q - p) (Physics.java:428-432).  Here d2 is
@@ -45,11 +47,10 @@ namespace plg {
 
 namespace {
 
-constexpr int kThreads = 256;       // literal-path kernel
-constexpr int kTileThreads = 128;   // tiled kernel: targets per block
-constexpr int kTileCap = 1280;      // staged candidates per segment
-constexpr int kTileCols = 160;      // segment columns incl. both halos
-constexpr int kSmemMatrixMax = 16;  // matrix in shared memory up to 16 x 16
+constexpr int kThreads = 256;        // literal-path and fixup kernels
+constexpr int kTileTargets = 128;    // targets per block of the tiled kernel (one thread each)
+constexpr int kTileThreads = kTileTargets;
+constexpr int kSmemMatrixMax = 16;   // matrix in shared memory up to 16 x 16
 
 template <int D>
 struct ForceArgs {
@@ -64,7 +65,6 @@ struct ForceArgs {
     uint32_t* counts;
     uint32_t* defer_count;  // deferred-target list: count, then slots
     uint32_t* defer_list;
-    const uint32_t* __restrict__ refslot;  // B slot -> slot in the reference order (A)
     DebugOut dbg;
 };
 
@@ -307,12 +307,11 @@ __device__ __forceinline__ float ensure_position(float x, int wrap) {
     return fminf(fmaxf(x, 0.f), 1.f);
 }
 
-// Epilogue of one target read from B slot s: v = v ff + acc (rmax force dt),
-// x = v dt + x, ensurePosition; the next state goes to A[o], o the slot of
-// this particle in the reference order.  Returns the new cell.
+// Epilogue of one target (sorted slot s): v = v ff + acc (rmax force dt),
+// x = v dt + x, ensurePosition; the next state goes to A[s].  Returns the
+// new cell.
 template <int D, bool DBG>
-__device__ __forceinline__ uint32_t integrate(const ForceArgs<D>& A, int s, int o, const float4& me,
-                                              const Acc& acc) {
+__device__ __forceinline__ uint32_t integrate(const ForceArgs<D>& A, int s, const float4& me, const Acc& acc) {
     const ForceParams& P = A.p;
     typename Layout<D>::Vel v = A.bvel[s];
     const float vx = fmaf(acc.x, P.scale, v.x * P.ff);
@@ -321,22 +320,22 @@ __device__ __forceinline__ uint32_t integrate(const ForceArgs<D>& A, int s, int 
     const float nyp = ensure_position(__fadd_rn(__fmul_rn(vy, P.dt), me.y), P.wrap);
     float nzp = 0.f;
     if constexpr (D == 2) {
-        A.apt[o] = make_float4(nxp, nyp, me.z, me.w);
-        A.avel[o] = make_float2(vx, vy);
+        A.apt[s] = make_float4(nxp, nyp, me.z, me.w);
+        A.avel[s] = make_float2(vx, vy);
     } else {
         const float vz = fmaf(acc.z, P.scale, v.z * P.ff);
         nzp = ensure_position(__fadd_rn(__fmul_rn(vz, P.dt), me.z), P.wrap);
-        A.apt[o] = make_float4(nxp, nyp, nzp, me.w);
-        A.avel[o] = make_float4(vx, vy, vz, v.w);
+        A.apt[s] = make_float4(nxp, nyp, nzp, me.w);
+        A.avel[s] = make_float4(vx, vy, vz, v.w);
     }
     if (DBG) {
-        if (A.dbg.pairs) A.dbg.pairs[o] = acc.pairs;
-        if (A.dbg.hsum) A.dbg.hsum[o] = acc.hs;
-        if (A.dbg.hxor) A.dbg.hxor[o] = acc.hx;
+        if (A.dbg.pairs) A.dbg.pairs[s] = acc.pairs;
+        if (A.dbg.hsum) A.dbg.hsum[s] = acc.hs;
+        if (A.dbg.hxor) A.dbg.hxor[s] = acc.hx;
         if (A.dbg.acc) {
-            A.dbg.acc[(size_t)D * o + 0] = acc.x;
-            A.dbg.acc[(size_t)D * o + 1] = acc.y;
-            if (D == 3) A.dbg.acc[(size_t)D * o + 2] = acc.z;
+            A.dbg.acc[(size_t)D * s + 0] = acc.x;
+            A.dbg.acc[(size_t)D * s + 1] = acc.y;
+            if (D == 3) A.dbg.acc[(size_t)D * s + 2] = acc.z;
         }
         if (A.dbg.candidates) atomicAdd(A.dbg.candidates, acc.cand);
     }
@@ -365,18 +364,16 @@ __global__ void __launch_bounds__(kThreads) k_force_general(const __grid_constan
     const int s = blockIdx.x * kThreads + threadIdx.x;
     const bool valid = s < P.n;
     uint32_t newcell = 0;
-    int o = 0;
     if (valid) {
         const float4 me = A.bpt[s];
-        o = (int)A.refslot[s];
         Acc acc = {0.f, 0.f, 0.f, 0, 0ull, 0ull, 0ull};
         general_scan<D, DBG>(A, M + Layout<D>::type(me) * P.ntypes, s, me.x, me.y, D == 3 ? me.z : 0.f, acc);
-        newcell = integrate<D, DBG>(A, s, o, me, acc);
+        newcell = integrate<D, DBG>(A, s, me, acc);
     }
     const unsigned mask = __ballot_sync(kFull, valid);
     if (valid) {
-        A.rank[o] = bin_count(A.counts, newcell, mask);
-        A.cell[o] = newcell;
+        A.rank[s] = bin_count(A.counts, newcell, mask);
+        A.cell[s] = newcell;
     }
 }
 
@@ -388,23 +385,79 @@ struct TileRows {
 };
 
 template <int D>
+struct TileCfg {
+    static constexpr int kCap = D == 3 ? 2560 : 1536;  // staged candidates per segment
+    static constexpr int kCells = 512;                   // stencil cells per segment (R x columns)
+};
+
+// Target shifts a staged candidate asks for (bits 16..18 of its type word):
+// the target uses x - 1 (y - 1, z - 1) against it, because the candidate is
+// the periodic image above the box of a cell near coordinate 0.
+constexpr int kShiftX = 1 << 16, kShiftY = 1 << 17, kShiftZ = 1 << 18;
+
+// Lives in dynamic shared memory (about 31 KB in 2D, 47 KB in 3D).
+template <int D>
 struct TileSmem {
-    static constexpr int R = TileRows<D>::R;
-    float4 cand[kTileCap];          // staged candidates (x, y, z|type, type|id)
-    int coff[R][kTileCols + 1];     // per stencil row: smem start of each column
-    int pst[R][4];                  // per row: smem start of left halo, main, right halo; end
-    int pgb[R][3];                  // per row: global start of the three pieces
-    float tshy[R], tshz[R];         // per row: 1 where the target must use y - 1 (z - 1)
-    int rowid[kTileThreads];
-    int colid[kTileThreads];
-    int seg[kTileThreads + 1];
-    int wsum[kTileThreads / 32];
+    float4 cand[TileCfg<D>::kCap];      // staged candidates, column-major by stencil cell
+    int coff[TileCfg<D>::kCells + 1];   // smem start of stencil cell e = column * R + row
+    int cglob[TileCfg<D>::kCells];      // sorted-order start of stencil cell e
+    float4 tpos[kTileTargets];          // the block's targets
+    int rowid[kTileTargets];
+    int colid[kTileTargets];
+    int seg[kTileTargets + 1];
+    int wsum[kTileTargets / 32];
     int nseg;
-    int staged;                     // 1: the segment's stencil is in smem
+    int staged;                         // 1: the segment's stencil is in smem
     float mat[kSmemMatrixMax * kSmemMatrixMax];
 };
 
-// Stages the stencil of the segment (grid row `srow`, columns cxa..cxb).
+__device__ __forceinline__ int wrap_index(int c, int n) { return c < 0 ? c + n : (c >= n ? c - n : c); }
+
+// Block-wide exclusive scan of v[0..n) in place (n <= kCells); returns the total.
+template <int D>
+__device__ __forceinline__ int block_scan_inplace(int* v, int n, int* wsum) {
+    constexpr int per = (TileCfg<D>::kCells + kTileThreads - 1) / kTileThreads;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    int loc[per];
+    int sum = 0;
+#pragma unroll
+    for (int i = 0; i < per; ++i) {
+        const int e = tid * per + i;
+        loc[i] = e < n ? v[e] : 0;
+        sum += loc[i];
+    }
+    int inc = sum;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const int t = __shfl_up_sync(kFull, inc, d);
+        if (lane >= d) inc += t;
+    }
+    if (lane == 31) wsum[warp] = inc;
+    __syncthreads();
+    int before = 0, total = 0;
+#pragma unroll
+    for (int w = 0; w < kTileThreads / 32; ++w) {
+        const int x = wsum[w];
+        before += w < warp ? x : 0;
+        total += x;
+    }
+    int run = before + inc - sum;
+#pragma unroll
+    for (int i = 0; i < per; ++i) {
+        const int e = tid * per + i;
+        if (e < n) v[e] = run;
+        run += loc[i];
+    }
+    __syncthreads();
+    return total;
+}
+
+// Stages the stencil of the segment (grid row `srow`, columns cxa..cxb),
+// column-major: for each stencil column (cxa-1 .. cxb+1) the cells of its R
+// stencil rows in turn, so that the neighbourhood of a target in column cx is
+// the single contiguous range of columns cx-1 .. cx+1.  Images below the box
+// are shifted down by 1 here (exact: their coordinates are >= 0.5); images
+// above it are flagged for a target shift instead.
 template <int D>
 __device__ __forceinline__ void stage_segment(const ForceArgs<D>& A, TileSmem<D>& sm, int srow, int cxa, int cxb) {
     constexpr int R = TileRows<D>::R;
@@ -413,106 +466,77 @@ __device__ __forceinline__ void stage_segment(const ForceArgs<D>& A, TileSmem<D>
     const int tid = threadIdx.x;
     const int cy = D == 3 ? srow % nx : srow, cz = D == 3 ? srow / nx : 0;
     const int ncols = cxb - cxa + 1;
+    const int ncell = R * (ncols + 2);
     const uint32_t* __restrict__ cs = A.cstart;
-    if (tid < 32) {
-        int lenL = 0, lenM = 0, lenR = 0, gL = 0, gM = 0, gR = 0;
-        float tsy = 0.f, tsz = 0.f;
-        if (tid < R) {
-            const int oy = tid % 3 - 1, oz = D == 3 ? tid / 3 - 1 : 0;
-            int ry = cy + oy, rz = cz + oz;
-            if (ry < 0) {
-                ry += nx;
-            } else if (ry >= nx) {
-                ry -= nx;
-                if (P.wrap) tsy = 1.f;
-            }
-            if (rz < 0) {
-                rz += nx;
-            } else if (rz >= nx) {
-                rz -= nx;
-                if (P.wrap) tsz = 1.f;
-            }
-            const int rb = (rz * nx + ry) * nx;
-            const int L = cxa > 0 ? cxa - 1 : nx - 1;
-            const int Rc = cxb < nx - 1 ? cxb + 1 : 0;
-            gL = (int)__ldg(cs + rb + L);
-            lenL = (int)__ldg(cs + rb + L + 1) - gL;
-            gM = (int)__ldg(cs + rb + cxa);
-            lenM = (int)__ldg(cs + rb + cxb + 1) - gM;
-            gR = (int)__ldg(cs + rb + Rc);
-            lenR = (int)__ldg(cs + rb + Rc + 1) - gR;
-        }
-        const int len = lenL + lenM + lenR;
-        int incl = len;
-#pragma unroll
-        for (int d = 1; d < 16; d <<= 1) {
-            const int t = __shfl_up_sync(kFull, incl, d);
-            if (tid >= d) incl += t;
-        }
-        const int total = __shfl_sync(kFull, incl, R - 1);
-        if (tid < R) {
-            const int base = incl - len;
-            sm.pst[tid][0] = base;
-            sm.pst[tid][1] = base + lenL;
-            sm.pst[tid][2] = base + lenL + lenM;
-            sm.pst[tid][3] = base + len;
-            sm.pgb[tid][0] = gL;
-            sm.pgb[tid][1] = gM;
-            sm.pgb[tid][2] = gR;
-            sm.tshy[tid] = tsy;
-            sm.tshz[tid] = tsz;
-        }
-        if (tid == 0) {
-            sm.staged = total <= kTileCap && ncols + 2 <= kTileCols;
-        }
+    if (ncell > TileCfg<D>::kCells) {
+        if (tid == 0) sm.staged = 0;
+        __syncthreads();
+        return;
+    }
+    for (int e = tid; e < ncell; e += kTileThreads) {
+        const int ci = e / R, r = e - ci * R;
+        const int col = wrap_index(cxa - 1 + ci, nx);
+        const int ry = wrap_index(cy + r % 3 - 1, nx);
+        const int rz = D == 3 ? wrap_index(cz + r / 3 - 1, nx) : 0;
+        const int c = (rz * nx + ry) * nx + col;
+        const int g0 = (int)__ldg(cs + c);
+        sm.cglob[e] = g0;
+        sm.coff[e] = (int)__ldg(cs + c + 1) - g0;
+    }
+    __syncthreads();
+    const int total = block_scan_inplace<D>(sm.coff, ncell, sm.wsum);
+    if (tid == 0) {
+        sm.coff[ncell] = total;
+        sm.staged = total <= TileCfg<D>::kCap;
     }
     __syncthreads();
     if (!sm.staged) return;
-    // Column starts: coff[r][0] = left halo, coff[r][1 + i] = column cxa + i,
-    // coff[r][ncols + 1] = right halo, coff[r][ncols + 2] = end.
-    const int w = ncols + 3;
-    for (int it = tid; it < R * w; it += kTileThreads) {
-        const int r = it / w, k = it - r * w;
-        int v;
-        if (k == 0) {
-            v = sm.pst[r][0];
-        } else if (k <= ncols + 1) {
+    for (int k = tid; k < total; k += kTileThreads) {
+        int lo = 0, hi = ncell;  // last e with coff[e] <= k
+        while (hi - lo > 1) {
+            const int m = (lo + hi) >> 1;
+            if (sm.coff[m] <= k)
+                lo = m;
+            else
+                hi = m;
+        }
+        const int e = lo, ci = e / R, r = e - ci * R;
+        float4 q = __ldg(A.bpt + sm.cglob[e] + (k - sm.coff[e]));
+        if (P.wrap) {
             const int oy = r % 3 - 1, oz = D == 3 ? r / 3 - 1 : 0;
-            int ry = cy + oy, rz = cz + oz;
-            ry = ry < 0 ? ry + nx : (ry >= nx ? ry - nx : ry);
-            rz = rz < 0 ? rz + nx : (rz >= nx ? rz - nx : rz);
-            v = sm.pst[r][1] + ((int)__ldg(cs + (rz * nx + ry) * nx + cxa + k - 1) - sm.pgb[r][1]);
-        } else {
-            v = sm.pst[r][3];
+            int flags = 0;
+            if (ci == 0 && cxa == 0) q.x -= 1.f;
+            if (ci == ncols + 1 && cxb == nx - 1) flags |= kShiftX;
+            if (cy + oy < 0) q.y -= 1.f;
+            if (cy + oy >= nx) flags |= kShiftY;
+            if (D == 3) {
+                if (cz + oz < 0) q.z -= 1.f;
+                if (cz + oz >= nx) flags |= kShiftZ;
+            }
+            if (flags) {
+                if constexpr (D == 2)
+                    q.z = __int_as_float(__float_as_int(q.z) | flags);
+                else
+                    q.w = __int_as_float(__float_as_int(q.w) | flags);
+            }
         }
-        sm.coff[r][k] = v;
-    }
-    // Candidates, with the exact periodic shifts of images below the box.
-    const float sxl = (cxa == 0 && P.wrap) ? -1.f : 0.f;
-#pragma unroll 1
-    for (int r = 0; r < R; ++r) {
-        const int oy = r % 3 - 1, oz = D == 3 ? r / 3 - 1 : 0;
-        const float sy = (cy + oy < 0 && P.wrap) ? -1.f : 0.f;
-        const float sz = (D == 3 && cz + oz < 0 && P.wrap) ? -1.f : 0.f;
-        const int p1 = sm.pst[r][1], p2 = sm.pst[r][2], p3 = sm.pst[r][3];
-        for (int k = sm.pst[r][0] + tid; k < p3; k += kTileThreads) {
-            const int piece = k < p1 ? 0 : (k < p2 ? 1 : 2);
-            const int g = sm.pgb[r][piece] + (k - (piece == 0 ? sm.pst[r][0] : (piece == 1 ? p1 : p2)));
-            float4 q = __ldg(A.bpt + g);
-            q.y += sy;
-            if (D == 3) q.z += sz;
-            if (piece == 0) q.x += sxl;
-            sm.cand[k] = q;
-        }
+        sm.cand[k] = q;
     }
     __syncthreads();
 }
 
-// Global sorted slot of staged candidate j of stencil row r.
+// Global sorted slot of staged candidate j (rare path and debug only).
 template <int D>
-__device__ __forceinline__ int staged_global(const TileSmem<D>& sm, int r, int j) {
-    const int piece = j < sm.pst[r][1] ? 0 : (j < sm.pst[r][2] ? 1 : 2);
-    return sm.pgb[r][piece] + (j - sm.pst[r][piece]);
+__device__ __forceinline__ int staged_global(const TileSmem<D>& sm, int ncell, int j) {
+    int lo = 0, hi = ncell;
+    while (hi - lo > 1) {
+        const int m = (lo + hi) >> 1;
+        if (sm.coff[m] <= j)
+            lo = m;
+        else
+            hi = m;
+    }
+    return sm.cglob[lo] + (j - sm.coff[lo]);
 }
 
 // rsqrt.approx.ftz.f32: the fast path only sees d2 >= 2^-100, a normal float.
@@ -522,17 +546,28 @@ __device__ __forceinline__ float rsqrt_approx(float x) {
     return r;
 }
 
-// First pass over staged candidates [j0, j1): branch-free, every lane runs
-// the FP32 Accelerator and keeps the term only for pairs decided inside.
-// Returns true when some candidate needs the FP64 decision (band or tiny).
-template <int D, bool DBG>
+// The target's neighbourhood: staged candidates [j0, j1).  Branch-free: every
+// lane runs the FP32 Accelerator and keeps the term only for pairs decided
+// inside.  SHIFT: the segment touches the box's upper boundary, so some
+// candidates carry target-shift flags.  Returns true when some candidate
+// needs the FP64 decision (band or tiny).
+template <int D, bool DBG, bool SHIFT>
 __device__ __forceinline__ bool tile_run(const ForceArgs<D>& A, const TileSmem<D>& sm, const float* __restrict__ Mrow,
-                                         int r, int j0, int j1, int self_j, float pxe, float pye, float pze,
+                                         int ncell, int j0, int j1, int self_j, float px, float py, float pz,
                                          Acc& acc) {
     const ForceParams& P = A.p;
+    const float px1 = px - 1.f, py1 = py - 1.f, pz1 = pz - 1.f;
     bool rare = false;
-    auto body = [&](int j) {
+    for (int j = j0; j < j1; ++j) {
         const float4 q = sm.cand[j];
+        int tb = __float_as_int(D == 3 ? q.w : q.z);
+        float pxe = px, pye = py, pze = pz;
+        if (SHIFT) {
+            pxe = (tb & kShiftX) ? px1 : px;
+            pye = (tb & kShiftY) ? py1 : py;
+            if (D == 3) pze = (tb & kShiftZ) ? pz1 : pz;
+            tb &= 0xffff;
+        }
         const float dx = q.x - pxe;
         const float dy = q.y - pye;
         float d2;
@@ -544,9 +579,9 @@ __device__ __forceinline__ bool tile_run(const ForceArgs<D>& A, const TileSmem<D
             d2 = fmaf(dx, dx, dy * dy);
         }
         const bool other = j != self_j;
-        const bool fast = other && d2 <= P.lo && d2 >= P.tiny;
-        rare |= other && !fast && d2 < P.hi;
-        const float a = Mrow[Layout<D>::type(q)];
+        const bool fast = other & (d2 <= P.lo) & (d2 >= P.tiny);
+        rare |= other & !fast & (d2 < P.hi);
+        const float a = Mrow[tb];
         const float inv = rsqrt_approx(d2);
         const float dist = d2 * inv;
         const float t = fmaf(dist, P.m2_inv_rmax, P.one_plus_beta);
@@ -558,45 +593,11 @@ __device__ __forceinline__ bool tile_run(const ForceArgs<D>& A, const TileSmem<D
         if (D == 3) acc.z = fmaf(dz, g, acc.z);
         if (DBG) {
             if (other) acc.cand++;
-            if (fast) add_pair<D, true>(acc, make_float4(0.f, 0.f, 0.f, 0.f), id_of<D>(A, staged_global(sm, r, j)));
+            if (fast)
+                add_pair<D, true>(acc, make_float4(0.f, 0.f, 0.f, 0.f), id_of<D>(A, staged_global(sm, ncell, j)));
         }
-    };
-    int j = j0;
-    for (; j + 4 <= j1; j += 4) {
-        body(j);
-        body(j + 1);
-        body(j + 2);
-        body(j + 3);
     }
-    for (; j < j1; ++j) body(j);
     return rare;
-}
-
-// First index in [a, b) whose staged x is >= v (> v when UPPER); NaN
-// coordinates, staged last, compare as above every bound.
-template <bool UPPER>
-__device__ __forceinline__ int search_x(const float4* cand, int a, int b, float v) {
-    while (a < b) {
-        const int m = (a + b) >> 1;
-        const float x = cand[m].x;
-        if (UPPER ? x <= v : x < v)
-            a = m + 1;
-        else
-            b = m;
-    }
-    return a;
-}
-
-// An x-sorted part [j0, j1) of a run, cut to the candidates within xwin of
-// the target in x: every pair that can pass d2 < hi has |dx| < xwin.
-template <int D, bool DBG>
-__device__ __forceinline__ bool window_run(const ForceArgs<D>& A, const TileSmem<D>& sm, const float* __restrict__ Mrow,
-                                           int r, int j0, int j1, int self_j, float pxe, float pye, float pze,
-                                           Acc& acc) {
-    if (j0 >= j1) return false;
-    const int a = search_x<false>(sm.cand, j0, j1, pxe - A.p.xwin);
-    const int b = search_x<true>(sm.cand, a, j1, pxe + A.p.xwin);
-    return tile_run<D, DBG>(A, sm, Mrow, r, a, b, self_j, pxe, pye, pze, acc);
 }
 
 // Appends the lanes with `want` to the deferred-target list (one atomic per
@@ -612,14 +613,17 @@ __device__ __forceinline__ void defer_targets(uint32_t* count, uint32_t* list, b
     if (want) list[base + __popc(m & ((1u << lane) - 1u))] = (uint32_t)s;
 }
 
-// Main force kernel (nx >= 3).  FP32 only and call-free: a target whose
-// first pass meets a candidate that needs the FP64 decision, or whose
-// segment did not fit in shared memory, is deferred to k_force_fixup, which
-// recomputes it completely.
+// Main force kernel (nx >= 3): one thread per target; a block takes 128
+// consecutive targets and, per segment (targets of one grid row), stages the
+// segment's stencil so that each target reads one contiguous run.  FP32 only
+// and call-free: a target whose run meets a candidate that needs the FP64
+// decision, or whose segment did not fit in shared memory, is deferred to
+// k_force_fixup, which recomputes it completely.
 template <int D, bool DBG, bool SMEM_M>
-__global__ void __launch_bounds__(kTileThreads, 8) k_force_tile(const ForceArgs<D> A) {
+__global__ void __launch_bounds__(kTileThreads) k_force_tile(const ForceArgs<D> A) {
     constexpr int R = TileRows<D>::R;
-    __shared__ TileSmem<D> sm;
+    extern __shared__ __align__(16) unsigned char smraw[];
+    TileSmem<D>& sm = *reinterpret_cast<TileSmem<D>*>(smraw);
     const ForceParams& P = A.p;
     const int tid = threadIdx.x;
     const int nx = P.g.nx;
@@ -628,18 +632,19 @@ __global__ void __launch_bounds__(kTileThreads, 8) k_force_tile(const ForceArgs<
         for (int k = tid; k < nn; k += kTileThreads) sm.mat[k] = P.matrix[k];
     }
     const float* M = SMEM_M ? sm.mat : P.matrix;
-    const int s = blockIdx.x * kTileThreads + tid;
-    const bool valid = s < P.n;
+    const int s0 = blockIdx.x * kTileTargets;
+    const int nvalid = min(kTileTargets, P.n - s0);
+    const bool valid = tid < nvalid;
+    const int s = s0 + tid;
     float4 me = make_float4(0.f, 0.f, 0.f, 0.f);
-    int cx = 0, cy = 0, cz = 0;
+    int cx = 0, row = INT_MAX;
     if (valid) {
         me = A.bpt[s];
         cx = axis_cell(me.x, P.g);
-        cy = axis_cell(me.y, P.g);
-        if (D == 3) cz = axis_cell(me.z, P.g);
+        const int cy = axis_cell(me.y, P.g);
+        const int cz = D == 3 ? axis_cell(me.z, P.g) : 0;
+        row = cy + cz * nx;
     }
-    const float px = me.x, py = me.y, pz = D == 3 ? me.z : 0.f;
-    const int row = valid ? cy + cz * nx : INT_MAX;
     sm.rowid[tid] = row;
     sm.colid[tid] = cx;
     __syncthreads();
@@ -653,45 +658,35 @@ __global__ void __launch_bounds__(kTileThreads, 8) k_force_tile(const ForceArgs<
     if (start) sm.seg[before + __popc(bal & ((1u << (tid & 31)) - 1u))] = tid;
     if (tid == 0) {
         int t = 0;
-        for (int w = 0; w < kTileThreads / 32; ++w) t += sm.wsum[w];
+        for (int w = 0; w < kTileTargets / 32; ++w) t += sm.wsum[w];
         sm.nseg = t;
-        sm.seg[t] = min(kTileThreads, P.n - (int)blockIdx.x * kTileThreads);
+        sm.seg[t] = nvalid;
     }
     __syncthreads();
     const int nseg = sm.nseg;
 
+    const float px = me.x, py = me.y, pz = D == 3 ? me.z : 0.f;
     const float* Mrow = M + (valid ? Layout<D>::type(me) : 0) * P.ntypes;
     Acc acc = {0.f, 0.f, 0.f, 0, 0ull, 0ull, 0ull};
     bool defer = false;
     for (int g = 0; g < nseg; ++g) {
         const int ta = sm.seg[g], tb = sm.seg[g + 1];
+        const int srow = sm.rowid[ta];
         const int cxa = sm.colid[ta], cxb = sm.colid[tb - 1];
-        stage_segment<D>(A, sm, sm.rowid[ta], cxa, cxb);
+        stage_segment<D>(A, sm, srow, cxa, cxb);
         if (tid >= ta && tid < tb) {
             if (sm.staged) {
-                const int ncols = cxb - cxa + 1;
-                const int k = cx - cxa + 1;
-                // Each cell is staged in x order and columns follow in x, so
-                // a run is x-sorted except for a halo column that wraps round
-                // the row: the left halo of column 0 (in order only when it
-                // is shifted down, i.e. periodic) and the right halo of
-                // column nx-1 (column 0's cells, reached through the target
-                // at x - 1 when periodic).  Those halos are separate parts.
-                const bool lsplit = cxa == 0 && k == 1;
-                const bool rsplit = cxb == nx - 1 && k == ncols;
-                const float pxr = P.wrap ? px - 1.f : px;
-#pragma unroll 1
-                for (int r = 0; r < R; ++r) {
-                    const float pye = py - sm.tshy[r];
-                    const float pze = pz - sm.tshz[r];
-                    const int j0 = sm.coff[r][k - 1], j1 = sm.coff[r][k + 2];
-                    const int jl = lsplit ? sm.coff[r][1] : j0;
-                    const int js = rsplit ? sm.coff[r][ncols + 1] : j1;
-                    const int self_j = r == R / 2 ? sm.pst[r][1] + (s - sm.pgb[r][1]) : -1;
-                    defer |= window_run<D, DBG>(A, sm, Mrow, r, j0, jl, self_j, px, pye, pze, acc);
-                    defer |= window_run<D, DBG>(A, sm, Mrow, r, jl, js, self_j, px, pye, pze, acc);
-                    defer |= window_run<D, DBG>(A, sm, Mrow, r, js, j1, self_j, pxr, pye, pze, acc);
-                }
+                const int ncell = R * (cxb - cxa + 3);
+                const int k = cx - cxa + 1;  // stencil column of the target
+                const int j0 = sm.coff[(k - 1) * R], j1 = sm.coff[(k + 2) * R];
+                const int own = k * R + R / 2;
+                const int self_j = sm.coff[own] + (s - sm.cglob[own]);
+                const int cy = D == 3 ? srow % nx : srow, cz = D == 3 ? srow / nx : 0;
+                const bool shift = P.wrap && (cxb == nx - 1 || cy == nx - 1 || (D == 3 && cz == nx - 1));
+                if (shift)
+                    defer = tile_run<D, DBG, true>(A, sm, Mrow, ncell, j0, j1, self_j, px, py, pz, acc);
+                else
+                    defer = tile_run<D, DBG, false>(A, sm, Mrow, ncell, j0, j1, self_j, px, py, pz, acc);
             } else {
                 defer = true;
             }
@@ -700,15 +695,11 @@ __global__ void __launch_bounds__(kTileThreads, 8) k_force_tile(const ForceArgs<
     }
     const bool done = valid && !defer;
     uint32_t newcell = 0;
-    int o = 0;
-    if (done) {
-        o = (int)A.refslot[s];
-        newcell = integrate<D, DBG>(A, s, o, me, acc);
-    }
+    if (done) newcell = integrate<D, DBG>(A, s, me, acc);
     const unsigned mask = __ballot_sync(kFull, done);
     if (done) {
-        A.rank[o] = bin_count(A.counts, newcell, mask);
-        A.cell[o] = newcell;
+        A.rank[s] = bin_count(A.counts, newcell, mask);
+        A.cell[s] = newcell;
     }
     defer_targets(A.defer_count, A.defer_list, valid && defer, s);
 }
@@ -757,10 +748,9 @@ __global__ void __launch_bounds__(kThreads) k_force_fixup(const __grid_constant_
             }
         }
         if (lane == 0) {
-            const int o = (int)A.refslot[s];
-            const uint32_t newcell = integrate<D, DBG>(A, s, o, me, acc);
-            A.rank[o] = atomicAdd(A.counts + newcell, 1u);
-            A.cell[o] = newcell;
+            const uint32_t newcell = integrate<D, DBG>(A, s, me, acc);
+            A.rank[s] = atomicAdd(A.counts + newcell, 1u);
+            A.cell[s] = newcell;
         }
     }
 }
@@ -777,11 +767,12 @@ void launch_variant(cudaStream_t st, const ForceArgs<D>& A, bool general, int fi
         else
             k_force_general<D, DBG, false><<<grid, kThreads, 0, st>>>(A);
     } else if (fixup_blocks == 0) {
-        const int grid = (n + kTileThreads - 1) / kTileThreads;
+        const int grid = (n + kTileTargets - 1) / kTileTargets;
+        const size_t sb = sizeof(TileSmem<D>);
         if (smem)
-            k_force_tile<D, DBG, true><<<grid, kTileThreads, 0, st>>>(A);
+            k_force_tile<D, DBG, true><<<grid, kTileThreads, sb, st>>>(A);
         else
-            k_force_tile<D, DBG, false><<<grid, kTileThreads, 0, st>>>(A);
+            k_force_tile<D, DBG, false><<<grid, kTileThreads, sb, st>>>(A);
     } else {
         if (smem)
             k_force_fixup<D, DBG, true><<<fixup_blocks, kThreads, 0, st>>>(A);
@@ -792,8 +783,7 @@ void launch_variant(cudaStream_t st, const ForceArgs<D>& A, bool general, int fi
 
 template <int D>
 ForceArgs<D> make_args(const ForceParams& p, StateBuf<D> b, const uint32_t* cstart, StateBuf<D> a, uint32_t* cell,
-                       uint32_t* rank, uint32_t* counts, uint32_t* defer, const uint32_t* refslot,
-                       const DebugOut* dbg) {
+                       uint32_t* rank, uint32_t* counts, uint32_t* defer, const DebugOut* dbg) {
     ForceArgs<D> A;
     A.p = p;
     A.bpt = b.pt;
@@ -806,7 +796,6 @@ ForceArgs<D> make_args(const ForceParams& p, StateBuf<D> b, const uint32_t* csta
     A.counts = counts;
     A.defer_count = defer;
     A.defer_list = defer + 1;
-    A.refslot = refslot;
     A.dbg = dbg ? *dbg : DebugOut{nullptr, nullptr, nullptr, nullptr, nullptr};
     return A;
 }
@@ -816,9 +805,9 @@ ForceArgs<D> make_args(const ForceParams& p, StateBuf<D> b, const uint32_t* csta
 template <int D>
 void launch_force(cudaStream_t st, const ForceParams& p, bool general, StateBuf<D> b, const uint32_t* cstart,
                   StateBuf<D> a, uint32_t* cell, uint32_t* rank, uint32_t* counts, uint32_t* defer,
-                  const uint32_t* refslot, const DebugOut* dbg) {
+                  const DebugOut* dbg) {
     if (p.n <= 0) return;
-    const ForceArgs<D> A = make_args<D>(p, b, cstart, a, cell, rank, counts, defer, refslot, dbg);
+    const ForceArgs<D> A = make_args<D>(p, b, cstart, a, cell, rank, counts, defer, dbg);
     if (dbg)
         launch_variant<D, true>(st, A, general, 0);
     else
@@ -828,9 +817,9 @@ void launch_force(cudaStream_t st, const ForceParams& p, bool general, StateBuf<
 template <int D>
 void launch_force_fixup(cudaStream_t st, const ForceParams& p, bool general, StateBuf<D> b, const uint32_t* cstart,
                         StateBuf<D> a, uint32_t* cell, uint32_t* rank, uint32_t* counts, uint32_t* defer,
-                        const uint32_t* refslot, const DebugOut* dbg, int blocks) {
+                        const DebugOut* dbg, int blocks) {
     if (p.n <= 0 || general) return;
-    const ForceArgs<D> A = make_args<D>(p, b, cstart, a, cell, rank, counts, defer, refslot, dbg);
+    const ForceArgs<D> A = make_args<D>(p, b, cstart, a, cell, rank, counts, defer, dbg);
     if (dbg)
         launch_variant<D, true>(st, A, false, blocks);
     else
@@ -838,15 +827,34 @@ void launch_force_fixup(cudaStream_t st, const ForceParams& p, bool general, Sta
 }
 
 template void launch_force<2>(cudaStream_t, const ForceParams&, bool, StateBuf<2>, const uint32_t*, StateBuf<2>,
-                              uint32_t*, uint32_t*, uint32_t*, uint32_t*, const uint32_t*, const DebugOut*);
+                              uint32_t*, uint32_t*, uint32_t*, uint32_t*, const DebugOut*);
 template void launch_force<3>(cudaStream_t, const ForceParams&, bool, StateBuf<3>, const uint32_t*, StateBuf<3>,
-                              uint32_t*, uint32_t*, uint32_t*, uint32_t*, const uint32_t*, const DebugOut*);
+                              uint32_t*, uint32_t*, uint32_t*, uint32_t*, const DebugOut*);
 template void launch_force_fixup<2>(cudaStream_t, const ForceParams&, bool, StateBuf<2>, const uint32_t*,
-                                    StateBuf<2>, uint32_t*, uint32_t*, uint32_t*, uint32_t*, const uint32_t*,
-                                    const DebugOut*, int);
+                                    StateBuf<2>, uint32_t*, uint32_t*, uint32_t*, uint32_t*, const DebugOut*,
+                                    int);
 template void launch_force_fixup<3>(cudaStream_t, const ForceParams&, bool, StateBuf<3>, const uint32_t*,
-                                    StateBuf<3>, uint32_t*, uint32_t*, uint32_t*, uint32_t*, const uint32_t*,
-                                    const DebugOut*, int);
+                                    StateBuf<3>, uint32_t*, uint32_t*, uint32_t*, uint32_t*, const DebugOut*,
+                                    int);
+
+template <int D>
+cudaError_t allow_tile_smem() {
+    const int sb = (int)sizeof(TileSmem<D>);
+    cudaError_t e = cudaFuncSetAttribute(k_force_tile<D, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sb);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_force_tile<D, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, sb);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_force_tile<D, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sb);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_force_tile<D, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, sb);
+    return e;
+}
+
+cudaError_t force_kernels_init() {
+    cudaError_t e = allow_tile_smem<2>();
+    if (e == cudaSuccess) e = allow_tile_smem<3>();
+    return e;
+}
 
 // ---- FP32 FMA throughput probe ----
 

@@ -111,7 +111,6 @@ struct ForceParams {
     int slmask_ok;          // nx >= 4: sliver targets need the stencil correction
     const float* matrix;    // ntypes x ntypes, row-major, FP32
     float lo, hi, tiny;     // FP32 d2 decision band around rmax^2
-    float xwin;             // > sqrt(hi) with margin: |dx| bound of any pair with d2 < hi
     float inv_rmax;
     float beta, inv_beta, one_plus_beta, inv_one_minus_beta;
     float m2_inv_rmax;      // -2 / rmax
@@ -163,19 +162,23 @@ void launch_scatter(cudaStream_t st, int n, const uint32_t* cell, const uint32_t
 
 template <int D>
 void launch_gather(cudaStream_t st, int n, const uint32_t* perm, const uint32_t* cell, const uint32_t* cstart,
-                   StateBuf<D> a, StateBuf<D> b, uint32_t* refslot, int32_t* cell_sorted);
+                   StateBuf<D> a, StateBuf<D> b, int32_t* cell_sorted);
 
 // `defer`: 1 + n words, word 0 zeroed before the step (deferred-target list).
 template <int D>
 void launch_force(cudaStream_t st, const ForceParams& p, bool general, StateBuf<D> b, const uint32_t* cstart,
                   StateBuf<D> a, uint32_t* cell, uint32_t* rank, uint32_t* counts, uint32_t* defer,
-                  const uint32_t* refslot, const DebugOut* dbg);
+                  const DebugOut* dbg);
 
 // Completes the targets k_force_tile deferred (no-op for nx < 3).
 template <int D>
 void launch_force_fixup(cudaStream_t st, const ForceParams& p, bool general, StateBuf<D> b, const uint32_t* cstart,
                         StateBuf<D> a, uint32_t* cell, uint32_t* rank, uint32_t* counts, uint32_t* defer,
-                        const uint32_t* refslot, const DebugOut* dbg, int blocks);
+                        const DebugOut* dbg, int blocks);
+
+// Opts the tiled force kernel in to its dynamic shared memory (> 48 KB) on
+// the current device; called once per context.
+cudaError_t force_kernels_init();
 
 cudaError_t probe_fp32_peak(double* tflops);
 

@@ -79,7 +79,6 @@ struct plg_ctx {
     uint32_t* rank = nullptr;
     uint32_t* perm = nullptr;
     uint32_t* defer = nullptr;  // deferred-target count + list (force -> fixup)
-    uint32_t* refslot = nullptr;  // B slot -> slot of the reference order
     int fixup_blocks = 0;
     unsigned char* stage = nullptr;
 
@@ -214,9 +213,6 @@ void compute_force_params(plg_ctx* c) {
     if ((double)hi < hi_d) hi = std::nextafter(hi, INFINITY);
     p.lo = lo;
     p.hi = hi;
-    // Every pair with FP32 d2 < hi has |dx| < sqrt(hi) (1 + 2^-24); the margin
-    // also covers the rounding of pxe +- xwin for coordinates in [-1, 1].
-    p.xwin = (float)(std::sqrt((double)hi) * (1.0 + std::ldexp(1.0, -10)) + std::ldexp(1.0, -22));
     p.tiny = std::ldexp(1.0f, -100);
     p.inv_rmax = (float)(1.0 / s.rmax);
     p.beta = (float)s.beta;
@@ -256,15 +252,15 @@ void enqueue_body(plg_ctx* c, const DebugOut* dbg, int32_t* cell_sorted) {
     launch_scatter(st, n, c->cell, c->rank, c->cstart, c->perm);
     k1(PLG_K_SCATTER);
     k0(PLG_K_GATHER);
-    launch_gather<D>(st, n, c->perm, c->cell, c->cstart, buf_a<D>(c), buf_b<D>(c), c->refslot, cell_sorted);
+    launch_gather<D>(st, n, c->perm, c->cell, c->cstart, buf_a<D>(c), buf_b<D>(c), cell_sorted);
     k1(PLG_K_GATHER);
     k0(PLG_K_FORCE);
     launch_force<D>(st, c->fp, c->general, buf_b<D>(c), c->cstart, buf_a<D>(c), c->cell, c->rank, c->counts,
-                    c->defer, c->refslot, dbg);
+                    c->defer, dbg);
     k1(PLG_K_FORCE);
     k0(PLG_K_FIXUP);
     launch_force_fixup<D>(st, c->fp, c->general, buf_b<D>(c), c->cstart, buf_a<D>(c), c->cell, c->rank, c->counts,
-                          c->defer, c->refslot, dbg, c->fixup_blocks);
+                          c->defer, dbg, c->fixup_blocks);
     k1(PLG_K_FIXUP);
 }
 
@@ -373,7 +369,7 @@ int read_status(plg_ctx* c) {
 int free_all(plg_ctx* c) {
     destroy_graph(c);
     void* ptrs[] = {c->bounds, c->counts, c->cstart, c->scan_state, c->matrix, c->apt, c->bpt, c->avel, c->bvel,
-                    c->cell, c->rank, c->perm, c->defer, c->refslot, c->stage, c->status_d, c->dbg_pairs, c->dbg_hsum, c->dbg_hxor,
+                    c->cell, c->rank, c->perm, c->defer, c->stage, c->status_d, c->dbg_pairs, c->dbg_hsum, c->dbg_hxor,
                     c->dbg_cand, c->dbg_acc, c->dbg_cell};
     for (void* p : ptrs)
         if (p) cudaFree(p);
@@ -468,6 +464,7 @@ int plg_create(int dim, int64_t capacity, plg_ctx** out) {
     if (e != cudaSuccess) rc = PLG_E_CUDA;
     int sms = 0;
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device) != cudaSuccess) rc = PLG_E_CUDA;
+    if (!rc && force_kernels_init() != cudaSuccess) rc = PLG_E_CUDA;
     // Deferred targets are rare (FP64 band pairs, overfull segments): one
     // wave of 256-thread blocks, capped by the capacity.
     c->fixup_blocks = (int)std::min<int64_t>(2 * (int64_t)sms, (capacity + 255) / 256);
@@ -479,7 +476,6 @@ int plg_create(int dim, int64_t capacity, plg_ctx** out) {
     dmalloc((void**)&c->rank, sizeof(uint32_t) * cap);
     dmalloc((void**)&c->perm, sizeof(uint32_t) * cap);
     dmalloc((void**)&c->defer, sizeof(uint32_t) * (cap + 1));
-    dmalloc((void**)&c->refslot, sizeof(uint32_t) * cap);
     dmalloc((void**)&c->stage, stage_bytes(capacity));
     dmalloc((void**)&c->status_d, 64);
     if (!rc && cudaMallocHost((void**)&c->status_h, 64) != cudaSuccess) rc = PLG_E_NO_MEMORY;

@@ -143,6 +143,22 @@ def test_2d_fast_particles_wrap_many_times(gpu):
     check_step(spec, gpu)
 
 
+def test_deferred_targets_are_rare_for_uniform_worlds(gpu):
+    """Only pairs within 2^-19 of rmax^2 (or coincident) need the FP64 path,
+    so the tiled kernel completes nearly every target itself."""
+    from plgpu.physics import GpuWorld
+
+    for dim, n, rmax in ((2, 400_000, 0.0025), (3, 200_000, 0.02)):
+        spec = uniform_world(n, 8, rmax, seed=15, dim=dim, vel_scale=0.01)
+        w = GpuWorld(dim, n)
+        w.set_settings(spec.rmax, spec.friction, spec.force, spec.dt, beta=spec.beta, wrap=spec.wrap)
+        w.set_matrix(spec.matrix)
+        w.upload(spec.pos, spec.vel, spec.types)
+        w.step(3)
+        assert w.deferred() < n * 1e-3
+        w.close()
+
+
 def test_2d_dense_clusters_overflow_shared_memory(gpu):
     """Clusters far denser than shared memory can stage: those targets take
     the deferred (global-memory) path."""
