@@ -197,6 +197,42 @@ int plg_step_stats(plg_ctx* ctx, int64_t* deferred);
  * TFLOP/s (an FFMA counts 2 flops).  Runs for about 0.1 s. */
 int plg_probe_fp32_peak(double* tflops);
 
+/* ---- cell sort without allocation ------------------------------------- */
+
+/* Capacity of plg_sort_cells_noalloc's fixed device scratch. */
+#define PLG_NOALLOC_MAX_PARTICLES (1 << 18)
+#define PLG_NOALLOC_MAX_CELLS (1 << 18)
+
+/* No counterpart in the reference.  Computes, for positions already in
+ * device memory, the stable cell-sorted order of makeContainers
+ * (Physics.java:309-354) with cells from getContainerIndex in FP64
+ * (Physics.java:362-375), and allocates nothing: its scratch is one fixed
+ * device array of about 4.2 MB per device, for callers that must not
+ * allocate device memory while they run (a frame loop owning its position
+ * buffer, where cudaFree would wait for the whole device; a fixed memory
+ * budget).
+ *   pos         device double[3n], PhysicsSnapshot layout (z unused in 2D)
+ *   perm        device uint32[n]: perm[s] = index of the particle at sorted
+ *               slot s; ties in a cell keep index order
+ *   cell_start  device uint32[nx^dim + 1], 16-byte aligned: first slot of
+ *               each cell, last = n
+ *   status      device uint32 or NULL; the caller zeroes it.  Kernels OR in
+ *               1 (a position outside [0,1] or NaN, clamped into the grid)
+ *               and 8 (a bounded device wait ran out)
+ *   stream      cudaStream_t to enqueue on (NULL: the default stream)
+ * Enqueues the work and returns.  n > PLG_NOALLOC_MAX_PARTICLES or
+ * nx^dim > PLG_NOALLOC_MAX_CELLS is rejected with PLG_E_CAPACITY, host or
+ * other-device pointers with PLG_E_INVALID_ARG, before anything is enqueued.
+ * The first call on a device sets up the scratch address for that device
+ * (cudaGetSymbolAddress, which may load the module): make it before any
+ * stream capture.  Each call zeroes its own counters on `stream`.  Calls
+ * that overlap in time on one device share the scratch and race: serialise
+ * them. */
+int plg_sort_cells_noalloc(int32_t dim, double rmax, int64_t n,
+                           const double* pos, uint32_t* perm,
+                           uint32_t* cell_start, uint32_t* status,
+                           void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -25,6 +25,8 @@ PLG_E_DEVICE = 8
 PLG_E_CAPACITY = 9
 
 PLG_ACCEL_PARTICLE_LIFE = 1
+PLG_NOALLOC_MAX_PARTICLES = 1 << 18
+PLG_NOALLOC_MAX_CELLS = 1 << 18
 
 KERNELS = ["scan", "scatter", "gather", "force", "fixup"]
 
@@ -83,6 +85,7 @@ SIGNATURES = {
     "plg_debug_step": (C.c_int, [_P, _I32P, _I32P, _U64P, _U64P, _FP, _I64P]),
     "plg_probe_fp32_peak": (C.c_int, [_DP]),
     "plg_step_stats": (C.c_int, [_P, _I64P]),
+    "plg_sort_cells_noalloc": (C.c_int, [C.c_int32, C.c_double, C.c_int64, _P, _P, _P, _P, _P]),
 }
 
 _lib = None
