@@ -298,9 +298,12 @@ def run_ours(args):
     flops = n * (cand * FLOPS_PER_CANDIDATE[2] + inter * FLOPS_PER_INTERACTION[2])
     achieved = flops / (force_us * 1e-6) / 1e12
     traffic = None
-    tf = REPO / "profiles" / "force_2d_1m_traffic.json"
+    tf = REPO / "profiles" / "k_force_tile_2d_1m.md"  # ncu summary of this kernel on this workload
     if tf.exists():
-        traffic = json.loads(tf.read_text()).get("dram_bytes_per_launch")
+        import re
+
+        mt = re.search(r"^dram_bytes_per_launch: (\d+)", tf.read_text(), re.M)
+        traffic = int(mt.group(1)) if mt else None
     roofline = {"bound": "fp32", "kernel": "force", "achieved": achieved, "peak": peak.value, "unit": "TFLOP/s",
                 "frac": achieved / peak.value, "traffic": traffic,
                 "peak_source": "FFMA microbenchmark run live by this bench (MEASURED_PEAKS.json has no FP32 peak)",

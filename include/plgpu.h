@@ -162,8 +162,7 @@ int plg_set_use_graph(plg_ctx* ctx, int32_t on);
 #define PLG_K_SCATTER 1 /* particle index -> its cell's range      */
 #define PLG_K_GATHER 2  /* stable in-cell order, A -> B            */
 #define PLG_K_FORCE 3   /* neighbour loop + integration + counting */
-#define PLG_K_FIXUP 4   /* targets the force kernel deferred       */
-#define PLG_K_COUNT 5
+#define PLG_K_COUNT 4
 
 /* When on, steps run as plain launches bracketed by CUDA events on the
  * context's stream; plg_profile_read returns per-kernel totals since the
@@ -188,8 +187,8 @@ int plg_debug_step(plg_ctx* ctx, int32_t* cell, int32_t* pairs,
                    uint64_t* hash_sum, uint64_t* hash_xor, float* acc,
                    int64_t* candidates);
 
-/* Targets of the last step that the tiled force kernel handed to the
- * global-memory fixup kernel (pairs needing the FP64 decision, or stencils
+/* Targets of the last step that the tiled force kernel recomputed in its
+ * closing global-memory pass (pairs needing the FP64 decision, or stencils
  * too large for shared memory).  Waits for the context's stream. */
 int plg_step_stats(plg_ctx* ctx, int64_t* deferred);
 

@@ -6,7 +6,8 @@
 // counts):
 //   scan      counts -> exclusive offsets (Physics.java:334-340), single
 //             pass with decoupled look-back; counts reset
-//   scatter   perm[cstart[cell]+rank] = i (unstable: atomics order warps)
+//   scatter   perm[cstart[cell]+rank] = i (unstable: atomics order warps),
+//             and the cell of that slot
 //   gather    rank_stable(i) = #{members of i's cell with a smaller index};
 //             B[cstart[cell] + rank_stable] = A[i]
 // The gather makes the sort stable, so the cell-sorted order equals the one
@@ -268,29 +269,36 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(uint32_t* __restrict__ co
 __global__ void __launch_bounds__(kThreads) k_scatter(int n, const uint32_t* __restrict__ cell,
                                                       const uint32_t* __restrict__ rank,
                                                       const uint32_t* __restrict__ cstart,
-                                                      uint32_t* __restrict__ perm) {
+                                                      uint32_t* __restrict__ perm, uint32_t* __restrict__ slot_cell) {
     const int i = blockIdx.x * kThreads + threadIdx.x;
     if (i >= n) return;
-    perm[cstart[cell[i]] + rank[i]] = (uint32_t)i;
+    const uint32_t c = cell[i];
+    const uint32_t slot = cstart[c] + rank[i];
+    perm[slot] = (uint32_t)i;
+    if (slot_cell) slot_cell[slot] = c;
 }
 
 // Places particle i = perm[s] at its rank among its cell's members by
 // index: the order of the reference's sequential scatter
 // (Physics.java:342-348).
+// slot_cell[s] is the cell of slot s (written by the scatter), so the
+// cell offsets and the particle's state load in parallel.
 template <int D>
 __global__ void __launch_bounds__(kThreads) k_gather(int n, const uint32_t* __restrict__ perm,
-                                                     const uint32_t* __restrict__ cell,
+                                                     const uint32_t* __restrict__ slot_cell,
                                                      const uint32_t* __restrict__ cstart, StateBuf<D> a,
                                                      StateBuf<D> b, int32_t* __restrict__ cell_sorted) {
     const int s = blockIdx.x * kThreads + threadIdx.x;
     if (s >= n) return;
     const uint32_t i = perm[s];
-    const uint32_t c = cell[i];
+    const uint32_t c = slot_cell[s];
     const uint32_t st = cstart[c], en = cstart[c + 1];
+    const float4 p = a.pt[i];
+    const typename Layout<D>::Vel v = a.vel[i];
     uint32_t r = 0;
     for (uint32_t t = st; t < en; ++t) r += __ldg(perm + t) < i ? 1u : 0u;
-    b.pt[st + r] = a.pt[i];
-    b.vel[st + r] = a.vel[i];
+    b.pt[st + r] = p;
+    b.vel[st + r] = v;
     if (cell_sorted) cell_sorted[st + r] = (int32_t)c;
 }
 
@@ -324,16 +332,16 @@ void launch_scan(cudaStream_t st, uint32_t* counts, int ncells, uint32_t* cstart
 }
 
 void launch_scatter(cudaStream_t st, int n, const uint32_t* cell, const uint32_t* rank, const uint32_t* cstart,
-                    uint32_t* perm) {
+                    uint32_t* perm, uint32_t* slot_cell) {
     if (n <= 0) return;
-    k_scatter<<<blocks_for(n, kThreads), kThreads, 0, st>>>(n, cell, rank, cstart, perm);
+    k_scatter<<<blocks_for(n, kThreads), kThreads, 0, st>>>(n, cell, rank, cstart, perm, slot_cell);
 }
 
 template <int D>
-void launch_gather(cudaStream_t st, int n, const uint32_t* perm, const uint32_t* cell, const uint32_t* cstart,
+void launch_gather(cudaStream_t st, int n, const uint32_t* perm, const uint32_t* slot_cell, const uint32_t* cstart,
                    StateBuf<D> a, StateBuf<D> b, int32_t* cell_sorted) {
     if (n <= 0) return;
-    k_gather<D><<<blocks_for(n, kThreads), kThreads, 0, st>>>(n, perm, cell, cstart, a, b, cell_sorted);
+    k_gather<D><<<blocks_for(n, kThreads), kThreads, 0, st>>>(n, perm, slot_cell, cstart, a, b, cell_sorted);
 }
 
 template void launch_upload<2>(cudaStream_t, int, const double*, const double*, const int32_t*, int, StateBuf<2>,

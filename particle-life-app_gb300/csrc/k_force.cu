@@ -8,8 +8,8 @@
 // and, in its epilogue, the counting pass of the next makeContainers
 // (Physics.java:328-332) on the new position.
 //
-// Tiling.  A block takes 128 consecutive targets of the sorted order, one
-// thread each.  Their cells are nondecreasing, so they fall into a few
+// Tiling.  A block takes 256 (3D: 128) consecutive targets of the sorted
+// order, one thread each.  Their cells are nondecreasing, so they fall into a few
 // "segments" (targets of one grid row: one y in 2D, one (y, z) in 3D).  For
 // each segment the block stages into shared memory, with coalesced loads, the
 // segment's stencil (3 rows in 2D, 9 in 3D, over the segment's columns plus a
@@ -17,7 +17,8 @@
 // a target in column cx is one contiguous run (columns cx-1..cx+1).  The
 // candidate loop is branch-free FP32.  A target that meets a candidate needing
 // the FP64 decision, or whose segment does not fit in shared memory, is
-// deferred to k_force_fixup (one warp per target, global-memory stencil).
+// deferred: at the end of the block one warp recomputes it from global
+// memory (fixup_target).
 //
 // Pair test.  The reference keeps a pair when d2 != 0 && d2 <= rmax*rmax in
 // FP64, with d = wrapConnection(q - p) (Physics.java:428-432).  Here d2 is
@@ -27,8 +28,11 @@
 // within 5 ulp of the FP64 one, so a pair with d2 <= lo is inside, a pair
 // with d2 >= hi is outside, and only pairs in the band (lo, hi) or below
 // `tiny` are re-decided with the reference's exact FP64 operation sequence
-// (rare_pair).  The interacting-pair set is therefore bit-identical to the
-// FP64 reference run on the same FP32 positions.
+// (fp64_keeps).  The interacting-pair set is therefore bit-identical to the
+// FP64 reference run on the same FP32 positions.  Only the decision is FP64:
+// the term of a kept band pair is FP32 like every other term (the force
+// vanishes at rmax, so it is tiny); only a pair whose FP32 d2 underflowed
+// (d2 < tiny, distinct particles closer than about 1e-15) takes the FP64 term.
 //
 // Stencil.  The reference scans the 9 (27) cells around floor(x/cs) without
 // clamping (Physics.java:404-409).  For a particle in the last partial cell
@@ -36,7 +40,7 @@
 // the binning cell; the two stencils differ only by column nx-2 (scanned
 // here, not there) and column 1 (scanned there, never within rmax).  A pair
 // of column nx-2 within rmax lies within 1e-15 relative of rmax^2, so it
-// reaches rare_pair, which rejects it like the reference.  Grids with fewer
+// reaches fp64_keeps, which rejects it like the reference.  Grids with fewer
 // than 3 cells per axis, where the reference visits a cell more than once,
 // take the literal path (general_scan).
 #include <climits>
@@ -48,8 +52,6 @@ namespace plg {
 namespace {
 
 constexpr int kThreads = 256;        // literal-path and fixup kernels
-constexpr int kTileTargets = 128;    // targets per block of the tiled kernel (one thread each)
-constexpr int kTileThreads = kTileTargets;
 constexpr int kSmemMatrixMax = 16;   // matrix in shared memory up to 16 x 16
 
 template <int D>
@@ -63,8 +65,7 @@ struct ForceArgs {
     uint32_t* __restrict__ cell;
     uint32_t* __restrict__ rank;
     uint32_t* counts;
-    uint32_t* defer_count;  // deferred-target list: count, then slots
-    uint32_t* defer_list;
+    uint32_t* defer_count;  // targets the tiled kernel deferred this step (statistics)
     DebugOut dbg;
 };
 
@@ -81,17 +82,18 @@ __device__ __forceinline__ double wrap_connection(double v) {
     return v;
 }
 
-// The reference's FP64 pair test and Accelerator on the raw FP32 positions
-// (upcast).  Returns (acc contribution, 1) if the pair interacts, w = 0 if
-// not.  `slmask` bit k: the target lies in the last partial cell of axis k
-// and nx >= 4, so candidates of cell nx-2 on that axis are outside the
-// reference's stencil.
+// The reference's FP64 pair test on the raw FP32 positions (upcast):
+// d = wrapConnection(q - p), keep when d2 != 0 && d2 <= rmax^2
+// (Physics.java:428-432), in the reference's operation order.  `slmask` bit
+// k: the target lies in the last partial cell of axis k and nx >= 4, so
+// candidates of cell nx-2 on that axis are outside the reference's stencil.
+// Writes the FP64 difference vector.
 template <int D>
-__device__ __noinline__ float4 rare_pair(const ForceParams& P, float px, float py, float pz, float4 q, float a,
-                                         int slmask) {
-    double dx = __dsub_rn((double)q.x, (double)px);
-    double dy = __dsub_rn((double)q.y, (double)py);
-    double dz = D == 3 ? __dsub_rn((double)q.z, (double)pz) : 0.0;
+__device__ __forceinline__ bool fp64_keeps(const ForceParams& P, float px, float py, float pz, float4 q, int slmask,
+                                           double& dx, double& dy, double& dz) {
+    dx = __dsub_rn((double)q.x, (double)px);
+    dy = __dsub_rn((double)q.y, (double)py);
+    dz = D == 3 ? __dsub_rn((double)q.z, (double)pz) : 0.0;
     if (P.wrap) {
         dx = wrap_connection(dx);
         dy = wrap_connection(dy);
@@ -99,14 +101,19 @@ __device__ __noinline__ float4 rare_pair(const ForceParams& P, float px, float p
     }
     // lengthSquared: x*x + (y*y + z*z), unfused.
     const double d2 = __dadd_rn(__dmul_rn(dx, dx), __dadd_rn(__dmul_rn(dy, dy), __dmul_rn(dz, dz)));
-    if (!(d2 != 0.0 && d2 <= P.rmax2)) return make_float4(0.f, 0.f, 0.f, 0.f);
+    if (!(d2 != 0.0 && d2 <= P.rmax2)) return false;
     if (slmask) {
         const int m2 = P.g.nx - 2;
-        if ((slmask & 1) && axis_cell(q.x, P.g) == m2) return make_float4(0.f, 0.f, 0.f, 0.f);
-        if ((slmask & 2) && axis_cell(q.y, P.g) == m2) return make_float4(0.f, 0.f, 0.f, 0.f);
-        if (D == 3 && (slmask & 4) && axis_cell(q.z, P.g) == m2) return make_float4(0.f, 0.f, 0.f, 0.f);
+        if ((slmask & 1) && axis_cell(q.x, P.g) == m2) return false;
+        if ((slmask & 2) && axis_cell(q.y, P.g) == m2) return false;
+        if (D == 3 && (slmask & 4) && axis_cell(q.z, P.g) == m2) return false;
     }
-    // relativePosition.div(rmax); accelerate(a, pos) (app/Main.java:275-280).
+    return true;
+}
+
+// The reference's Accelerator term in FP64 for a kept pair:
+// relativePosition.div(rmax); accelerate(a, pos) (app/Main.java:275-280).
+__device__ __noinline__ float4 fp64_term(const ForceParams& P, double dx, double dy, double dz, float a) {
     const double rx = __ddiv_rn(dx, P.rmax), ry = __ddiv_rn(dy, P.rmax), rz = __ddiv_rn(dz, P.rmax);
     const double dist = __dsqrt_rn(__dadd_rn(__dmul_rn(rx, rx), __dadd_rn(__dmul_rn(ry, ry), __dmul_rn(rz, rz))));
     const double beta = P.beta_d;
@@ -119,6 +126,16 @@ __device__ __noinline__ float4 rare_pair(const ForceParams& P, float px, float p
     }
     const double k = __ddiv_rn(f, dist);
     return make_float4((float)__dmul_rn(rx, k), (float)__dmul_rn(ry, k), (float)__dmul_rn(rz, k), 1.f);
+}
+
+// FP64 decision and FP64 term (the literal path for nx < 3): returns
+// (term, 1) when the pair interacts, w = 0 when not.
+template <int D>
+__device__ __noinline__ float4 rare_pair(const ForceParams& P, float px, float py, float pz, float4 q, float a,
+                                         int slmask) {
+    double dx, dy, dz;
+    if (!fp64_keeps<D>(P, px, py, pz, q, slmask, dx, dy, dz)) return make_float4(0.f, 0.f, 0.f, 0.f);
+    return fp64_term(P, dx, dy, dz, a);
 }
 
 template <int D, bool DBG>
@@ -156,98 +173,128 @@ __device__ __forceinline__ void fast_pair(const ForceParams& P, float a, float d
     acc.z = fmaf(dz, g, acc.z);
 }
 
-// ---- global-memory stencil (fallback of the tiled kernel) ----
+// ---- global-memory stencil of one target, one warp (fixup of the tiled kernel) ----
 
-// Candidates j0 + lane, j0 + lane + step, ... < j1 of one run of consecutive
-// cells.  (pxe, pye, pze): target position, minus 1 on an axis where the run
-// is the periodic image above the box; qo*: -1 on an axis where the run's own
-// coordinates must be shifted down (image below the box).  SHQ: some qo* != 0.
-template <int D, bool DBG, bool SHQ>
-__device__ __forceinline__ void scan_run(const ForceArgs<D>& A, const float* __restrict__ Mrow, int s, int j0,
-                                         int j1, float pxe, float pye, float pze, float qox, float qoy, float qoz,
-                                         float px, float py, float pz, int slmask, int lane, int step, Acc& acc) {
+// nx >= 3: each row (and layer) of the stencil is at most two runs of the
+// sorted order: cells cx-1..cx+1, split in two where the row wraps in x.
+// Lane k < 2R (R = 3 rows in 2D, 9 in 3D) describes run k (row k/2, part
+// k%2): its first slot, length and periodic shifts; a warp scan gives run
+// offsets, and the warp walks the concatenated runs 32 candidates at a time,
+// each lane finding its run by a binary search over the offsets.  All
+// descriptor loads of a target are issued at once.
+//   target side   (pxe, pye, pze): target position, minus 1 on an axis where
+//                 the run is the periodic image above the box
+//   candidate     (qox, qoy, qoz): -1 on an axis where the run's own
+//                 coordinates are shifted down (image below the box)
+template <int D, bool DBG>
+__device__ __noinline__ Acc warp_stencil(const ForceArgs<D>& A, const float* Mrow, int s, float px, float py,
+                                         float pz, int slmask, int lane) {
+    constexpr int R = D == 3 ? 9 : 3;
     const ForceParams& P = A.p;
-    for (int j = j0 + lane; j < j1; j += step) {
+    const int nx = P.g.nx;
+    const int cx = axis_cell(px, P.g), cy = axis_cell(py, P.g), cz = D == 3 ? axis_cell(pz, P.g) : 0;
+    int j0 = 0, len = 0;
+    float pxe = px, pye = py, pze = pz, qox = 0.f, qoy = 0.f, qoz = 0.f;
+    if (lane < 2 * R) {
+        const int row = lane >> 1, part = lane & 1;
+        int ry = cy + row % 3 - 1, rz = D == 3 ? cz + row / 3 - 1 : 0;
+        if (ry < 0) {
+            ry += nx;
+            if (P.wrap) qoy = -1.f;
+        } else if (ry >= nx) {
+            ry -= nx;
+            if (P.wrap) pye = py - 1.f;
+        }
+        if (D == 3) {
+            if (rz < 0) {
+                rz += nx;
+                if (P.wrap) qoz = -1.f;
+            } else if (rz >= nx) {
+                rz -= nx;
+                if (P.wrap) pze = pz - 1.f;
+            }
+        }
+        const int base = (rz * nx + ry) * nx;
+        int ca = 0, cb = 0;  // cells [ca, cb) of this row
+        if (cx >= 1 && cx <= nx - 2) {
+            if (part == 0) ca = cx - 1, cb = cx + 2;
+        } else if (cx == 0) {
+            if (part == 0) {
+                ca = nx - 1, cb = nx;
+                if (P.wrap) qox = -1.f;
+            } else {
+                ca = 0, cb = 2;
+            }
+        } else {
+            if (part == 0) {
+                ca = nx - 2, cb = nx;
+            } else {
+                ca = 0, cb = 1;
+                if (P.wrap) pxe = px - 1.f;
+            }
+        }
+        if (cb > ca) {
+            j0 = (int)__ldg(A.cstart + base + ca);
+            len = (int)__ldg(A.cstart + base + cb) - j0;
+        }
+    }
+    int inc = len;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const int t = __shfl_up_sync(kFull, inc, d);
+        if (lane >= d) inc += t;
+    }
+    const int off = inc - len;
+    const int total = __shfl_sync(kFull, inc, 31);
+    Acc acc = {0.f, 0.f, 0.f, 0, 0ull, 0ull, 0ull};
+    for (int k0 = 0; k0 < total; k0 += 32) {
+        const int k = k0 + lane;
+        int r = 0;  // last run with off <= k (lanes >= 2R have off = total)
+#pragma unroll
+        for (int step = 16; step > 0; step >>= 1) {
+            const int o = __shfl_sync(kFull, off, r + step);
+            if (o <= k) r += step;
+        }
+        const int rj0 = __shfl_sync(kFull, j0, r), roff = __shfl_sync(kFull, off, r);
+        const float tx = __shfl_sync(kFull, pxe, r), ty = __shfl_sync(kFull, pye, r);
+        const float sx = __shfl_sync(kFull, qox, r), sy = __shfl_sync(kFull, qoy, r);
+        float tz = 0.f, sz = 0.f;
+        if (D == 3) {
+            tz = __shfl_sync(kFull, pze, r);
+            sz = __shfl_sync(kFull, qoz, r);
+        }
+        if (k >= total) continue;
+        const int j = rj0 + (k - roff);
+        if (j == s) continue;
         const float4 q = __ldg(A.bpt + j);
-        const float dx = (SHQ ? q.x + qox : q.x) - pxe;
-        const float dy = (SHQ ? q.y + qoy : q.y) - pye;
+        const float dx = (q.x + sx) - tx;
+        const float dy = (q.y + sy) - ty;
         float d2;
         float dz = 0.f;
         if (D == 3) {
-            dz = (SHQ ? q.z + qoz : q.z) - pze;
+            dz = (q.z + sz) - tz;
             d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
         } else {
             d2 = fmaf(dx, dx, dy * dy);
         }
-        const bool other = j != s;
-        if (DBG && other) acc.cand++;
-        if (other && d2 <= P.lo && d2 >= P.tiny) {
-            fast_pair(P, Mrow[Layout<D>::type(q)], dx, dy, dz, d2, acc);
-            if (DBG) add_pair<D, true>(acc, make_float4(0.f, 0.f, 0.f, 0.f), id_of<D>(A, j));
-        } else if (other && d2 < P.hi) {
-            const float4 c = rare_pair<D>(P, px, py, pz, q, Mrow[Layout<D>::type(q)], slmask);
-            if (c.w != 0.f) add_pair<D, DBG>(acc, c, DBG ? id_of<D>(A, j) : 0ull);
+        if (DBG) acc.cand++;
+        // FP32 decides where it can; the band (lo, hi) and d2 < tiny are
+        // decided in FP64.  A kept pair's term is FP32 unless its FP32 d2
+        // lost the difference (d2 < tiny), where only FP64 resolves it.
+        bool keep = d2 <= P.lo && d2 >= P.tiny;
+        bool f64 = false;
+        double ddx = 0.0, ddy = 0.0, ddz = 0.0;
+        if (!keep && d2 < P.hi) {
+            keep = fp64_keeps<D>(P, px, py, pz, q, slmask, ddx, ddy, ddz);
+            f64 = d2 < P.tiny;
         }
-    }
-}
-
-template <int D, bool DBG>
-__device__ __forceinline__ void run(const ForceArgs<D>& A, const float* Mrow, int s, int j0, int j1, float pxe,
-                                    float pye, float pze, float qox, float qoy, float qoz, float px, float py,
-                                    float pz, int slmask, int lane, int step, Acc& acc) {
-    if (qox != 0.f || qoy != 0.f || qoz != 0.f) {
-        scan_run<D, DBG, true>(A, Mrow, s, j0, j1, pxe, pye, pze, qox, qoy, qoz, px, py, pz, slmask, lane, step, acc);
-    } else {
-        scan_run<D, DBG, false>(A, Mrow, s, j0, j1, pxe, pye, pze, 0.f, 0.f, 0.f, px, py, pz, slmask, lane, step,
-                                acc);
-    }
-}
-
-// nx >= 3: per row (and layer) of the stencil, the three cells cx-1..cx+1 are
-// one run of the sorted order unless the row wraps in x.  This lane takes
-// every step-th candidate of each run from its offset `lane`.
-template <int D, bool DBG>
-__device__ __noinline__ Acc stencil_scan(const ForceArgs<D>& A, const float* Mrow, int s, float px, float py,
-                                         float pz, int slmask, int lane, int step) {
-    const ForceParams& P = A.p;
-    Acc acc = {0.f, 0.f, 0.f, 0, 0ull, 0ull, 0ull};
-    const int nx = P.g.nx;
-    const int cx = axis_cell(px, P.g), cy = axis_cell(py, P.g), cz = D == 3 ? axis_cell(pz, P.g) : 0;
-    const uint32_t* __restrict__ cs = A.cstart;
-    for (int oz = (D == 3 ? -1 : 0); oz <= (D == 3 ? 1 : 0); ++oz) {
-        int rz = cz + oz;
-        float qoz = 0.f, pze = pz;
-        if (rz < 0) {
-            rz += nx;
-            if (P.wrap) qoz = -1.f;
-        } else if (rz >= nx) {
-            rz -= nx;
-            if (P.wrap) pze = pz - 1.f;
-        }
-        for (int oy = -1; oy <= 1; ++oy) {
-            int ry = cy + oy;
-            float qoy = 0.f, pye = py;
-            if (ry < 0) {
-                ry += nx;
-                if (P.wrap) qoy = -1.f;
-            } else if (ry >= nx) {
-                ry -= nx;
-                if (P.wrap) pye = py - 1.f;
-            }
-            const int row = (rz * nx + ry) * nx;
-            if (cx >= 1 && cx <= nx - 2) {
-                run<D, DBG>(A, Mrow, s, __ldg(cs + row + cx - 1), __ldg(cs + row + cx + 2), px, pye, pze, 0.f, qoy,
-                            qoz, px, py, pz, slmask, lane, step, acc);
-            } else if (cx == 0) {
-                run<D, DBG>(A, Mrow, s, __ldg(cs + row + nx - 1), __ldg(cs + row + nx), px, pye, pze,
-                            P.wrap ? -1.f : 0.f, qoy, qoz, px, py, pz, slmask, lane, step, acc);
-                run<D, DBG>(A, Mrow, s, __ldg(cs + row), __ldg(cs + row + 2), px, pye, pze, 0.f, qoy, qoz, px, py,
-                            pz, slmask, lane, step, acc);
+        if (keep) {
+            const float a = Mrow[Layout<D>::type(q)];
+            if (f64) {
+                add_pair<D, DBG>(acc, fp64_term(P, ddx, ddy, ddz, a), DBG ? id_of<D>(A, j) : 0ull);
             } else {
-                run<D, DBG>(A, Mrow, s, __ldg(cs + row + nx - 2), __ldg(cs + row + nx), px, pye, pze, 0.f, qoy,
-                            qoz, px, py, pz, slmask, lane, step, acc);
-                run<D, DBG>(A, Mrow, s, __ldg(cs + row), __ldg(cs + row + 1), P.wrap ? px - 1.f : px, pye, pze, 0.f,
-                            qoy, qoz, px, py, pz, slmask, lane, step, acc);
+                fast_pair(P, a, dx, dy, dz, d2, acc);
+                if (DBG) add_pair<D, true>(acc, make_float4(0.f, 0.f, 0.f, 0.f), id_of<D>(A, j));
             }
         }
     }
@@ -386,7 +433,9 @@ struct TileRows {
 
 template <int D>
 struct TileCfg {
-    static constexpr int kCap = D == 3 ? 2560 : 1536;  // staged candidates per segment
+    static constexpr int kTargets = D == 3 ? 128 : 256;  // targets per block, one thread each
+    static constexpr int kMinBlocks = D == 3 ? 4 : 6;    // resident blocks per SM the smem allows
+    static constexpr int kCap = D == 3 ? 2560 : 1536;    // staged candidates per segment
     static constexpr int kCells = 512;                   // stencil cells per segment (R x columns)
 };
 
@@ -401,11 +450,10 @@ struct TileSmem {
     float4 cand[TileCfg<D>::kCap];      // staged candidates, column-major by stencil cell
     int coff[TileCfg<D>::kCells + 1];   // smem start of stencil cell e = column * R + row
     int cglob[TileCfg<D>::kCells];      // sorted-order start of stencil cell e
-    float4 tpos[kTileTargets];          // the block's targets
-    int rowid[kTileTargets];
-    int colid[kTileTargets];
-    int seg[kTileTargets + 1];
-    int wsum[kTileTargets / 32];
+    int rowid[TileCfg<D>::kTargets];
+    int colid[TileCfg<D>::kTargets];
+    int seg[TileCfg<D>::kTargets + 1];
+    int wsum[TileCfg<D>::kTargets / 32];
     int nseg;
     int staged;                         // 1: the segment's stencil is in smem
     float mat[kSmemMatrixMax * kSmemMatrixMax];
@@ -416,7 +464,8 @@ __device__ __forceinline__ int wrap_index(int c, int n) { return c < 0 ? c + n :
 // Block-wide exclusive scan of v[0..n) in place (n <= kCells); returns the total.
 template <int D>
 __device__ __forceinline__ int block_scan_inplace(int* v, int n, int* wsum) {
-    constexpr int per = (TileCfg<D>::kCells + kTileThreads - 1) / kTileThreads;
+    constexpr int kT = TileCfg<D>::kTargets;
+    constexpr int per = (TileCfg<D>::kCells + kT - 1) / kT;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     int loc[per];
     int sum = 0;
@@ -436,7 +485,7 @@ __device__ __forceinline__ int block_scan_inplace(int* v, int n, int* wsum) {
     __syncthreads();
     int before = 0, total = 0;
 #pragma unroll
-    for (int w = 0; w < kTileThreads / 32; ++w) {
+    for (int w = 0; w < kT / 32; ++w) {
         const int x = wsum[w];
         before += w < warp ? x : 0;
         total += x;
@@ -473,7 +522,7 @@ __device__ __forceinline__ void stage_segment(const ForceArgs<D>& A, TileSmem<D>
         __syncthreads();
         return;
     }
-    for (int e = tid; e < ncell; e += kTileThreads) {
+    for (int e = tid; e < ncell; e += TileCfg<D>::kTargets) {
         const int ci = e / R, r = e - ci * R;
         const int col = wrap_index(cxa - 1 + ci, nx);
         const int ry = wrap_index(cy + r % 3 - 1, nx);
@@ -491,7 +540,7 @@ __device__ __forceinline__ void stage_segment(const ForceArgs<D>& A, TileSmem<D>
     }
     __syncthreads();
     if (!sm.staged) return;
-    for (int k = tid; k < total; k += kTileThreads) {
+    for (int k = tid; k < total; k += TileCfg<D>::kTargets) {
         int lo = 0, hi = ncell;  // last e with coff[e] <= k
         while (hi - lo > 1) {
             const int m = (lo + hi) >> 1;
@@ -546,19 +595,27 @@ __device__ __forceinline__ float rsqrt_approx(float x) {
     return r;
 }
 
-// The target's neighbourhood: staged candidates [j0, j1).  Branch-free: every
-// lane runs the FP32 Accelerator and keeps the term only for pairs decided
-// inside.  SHIFT: the segment touches the box's upper boundary, so some
-// candidates carry target-shift flags.  Returns true when some candidate
-// needs the FP64 decision (band or tiny).
+// Staged candidates [ja, jb) of the target (a part of its neighbourhood
+// without the target itself).  Branch-free FP32: every lane evaluates the
+// Accelerator for every candidate.  A pair beyond rmax needs no select: for
+// d2 >= hi the triangle factor u = 1 - |1 + beta - 2 d/rmax| / (1 - beta) is
+// below -1e-6 even after FP32 rounding, so max(u, 0) = 0 and the term is an
+// exact zero.  Pairs inside the decision band (lo, hi) or below `tiny`
+// (including other particles at the same position) make the function return
+// true: the caller then defers the target to the FP64 fixup, which discards
+// this partial sum.  SHIFT: the segment touches the box's upper boundary,
+// so some candidates carry target-shift flags.
 template <int D, bool DBG, bool SHIFT>
-__device__ __forceinline__ bool tile_run(const ForceArgs<D>& A, const TileSmem<D>& sm, const float* __restrict__ Mrow,
-                                         int ncell, int j0, int j1, int self_j, float px, float py, float pz,
-                                         Acc& acc) {
+__device__ __forceinline__ bool tile_range(const ForceArgs<D>& A, const TileSmem<D>& sm,
+                                           const float* __restrict__ Mrow, int ncell, int ja, int jb, float px,
+                                           float py, float pz, Acc& acc) {
     const ForceParams& P = A.p;
     const float px1 = px - 1.f, py1 = py - 1.f, pz1 = pz - 1.f;
     bool rare = false;
-    for (int j = j0; j < j1; ++j) {
+    // Loop constants in registers (read once, not per candidate).
+    const float c_lo = P.lo, c_hi = P.hi, c_tiny = P.tiny, c_m2 = P.m2_inv_rmax, c_opb = P.one_plus_beta;
+    const float c_iomb = P.inv_one_minus_beta, c_brm = P.beta_rmax, c_k1 = P.k1;
+    for (int j = ja; j < jb; ++j) {
         const float4 q = sm.cand[j];
         int tb = __float_as_int(D == 3 ? q.w : q.z);
         float pxe = px, pye = py, pze = pz;
@@ -578,49 +635,71 @@ __device__ __forceinline__ bool tile_run(const ForceArgs<D>& A, const TileSmem<D
         } else {
             d2 = fmaf(dx, dx, dy * dy);
         }
-        const bool other = j != self_j;
-        const bool fast = other & (d2 <= P.lo) & (d2 >= P.tiny);
-        rare |= other & !fast & (d2 < P.hi);
+        rare |= ((d2 > c_lo) & (d2 < c_hi)) | (d2 < c_tiny);
         const float a = Mrow[tb];
         const float inv = rsqrt_approx(d2);
         const float dist = d2 * inv;
-        const float t = fmaf(dist, P.m2_inv_rmax, P.one_plus_beta);
-        const float u = fmaf(-fabsf(t), P.inv_one_minus_beta, 1.f);
-        float g = dist < P.beta_rmax ? P.k1 - inv : (a * inv) * u;
-        g = fast ? g : 0.f;
+        const float t = fmaf(dist, c_m2, c_opb);
+        const float u = fmaxf(fmaf(-fabsf(t), c_iomb, 1.f), 0.f);
+        const float g = dist < c_brm ? c_k1 - inv : (a * inv) * u;
         acc.x = fmaf(dx, g, acc.x);
         acc.y = fmaf(dy, g, acc.y);
         if (D == 3) acc.z = fmaf(dz, g, acc.z);
         if (DBG) {
-            if (other) acc.cand++;
-            if (fast)
+            acc.cand++;
+            if ((d2 <= c_lo) & (d2 >= c_tiny))
                 add_pair<D, true>(acc, make_float4(0.f, 0.f, 0.f, 0.f), id_of<D>(A, staged_global(sm, ncell, j)));
         }
     }
     return rare;
 }
 
-// Appends the lanes with `want` to the deferred-target list (one atomic per
-// warp); every lane of the warp must call.
-__device__ __forceinline__ void defer_targets(uint32_t* count, uint32_t* list, bool want, int s) {
-    const unsigned m = __ballot_sync(kFull, want);
-    if (!m) return;
-    const int lane = threadIdx.x & 31;
-    const int leader = __ffs(m) - 1;
-    uint32_t base = 0;
-    if (lane == leader) base = atomicAdd(count, (uint32_t)__popc(m));
-    base = __shfl_sync(kFull, base, leader);
-    if (want) list[base + __popc(m & ((1u << lane) - 1u))] = (uint32_t)s;
+// Sum of `v` over the warp in a fixed butterfly order (the same bits on
+// every run); every lane receives the total.
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) v += __shfl_xor_sync(kFull, v, d);
+    return v;
 }
 
-// Main force kernel (nx >= 3): one thread per target; a block takes 128
+// One deferred target, one warp: the lanes split the candidates of the
+// global-memory stencil (with the FP64 decisions), their partial sums are
+// combined by warp_sum, and lane 0 runs the epilogue and the counting step.
+template <int D, bool DBG>
+__device__ __noinline__ void fixup_target(const ForceArgs<D>& A, const float* M, int s, int lane) {
+    const ForceParams& P = A.p;
+    const float4 me = A.bpt[s];
+    const float px = me.x, py = me.y, pz = D == 3 ? me.z : 0.f;
+    Acc acc = warp_stencil<D, DBG>(A, M + Layout<D>::type(me) * P.ntypes, s, px, py, pz,
+                                   sliver_mask<D>(P, px, py, pz), lane);
+    acc.x = warp_sum(acc.x);
+    acc.y = warp_sum(acc.y);
+    if (D == 3) acc.z = warp_sum(acc.z);
+    if (DBG) {
+#pragma unroll
+        for (int d = 16; d > 0; d >>= 1) {
+            acc.pairs += __shfl_xor_sync(kFull, acc.pairs, d);
+            acc.hs += __shfl_xor_sync(kFull, acc.hs, d);
+            acc.hx ^= __shfl_xor_sync(kFull, acc.hx, d);
+            acc.cand += __shfl_xor_sync(kFull, acc.cand, d);
+        }
+    }
+    if (lane == 0) {
+        const uint32_t newcell = integrate<D, DBG>(A, s, me, acc);
+        A.rank[s] = atomicAdd(A.counts + newcell, 1u);
+        A.cell[s] = newcell;
+    }
+}
+
+// Main force kernel (nx >= 3): one thread per target; a block takes 256 (3D: 128)
 // consecutive targets and, per segment (targets of one grid row), stages the
 // segment's stencil so that each target reads one contiguous run.  FP32 only
 // and call-free: a target whose run meets a candidate that needs the FP64
 // decision, or whose segment did not fit in shared memory, is deferred to
-// k_force_fixup, which recomputes it completely.
+// the block's closing pass (fixup_target), which recomputes it completely.
 template <int D, bool DBG, bool SMEM_M>
-__global__ void __launch_bounds__(kTileThreads) k_force_tile(const ForceArgs<D> A) {
+__global__ void __launch_bounds__(TileCfg<D>::kTargets, TileCfg<D>::kMinBlocks) k_force_tile(const __grid_constant__ ForceArgs<D> A) {
+    constexpr int kT = TileCfg<D>::kTargets;
     constexpr int R = TileRows<D>::R;
     extern __shared__ __align__(16) unsigned char smraw[];
     TileSmem<D>& sm = *reinterpret_cast<TileSmem<D>*>(smraw);
@@ -629,11 +708,11 @@ __global__ void __launch_bounds__(kTileThreads) k_force_tile(const ForceArgs<D> 
     const int nx = P.g.nx;
     if (SMEM_M) {
         const int nn = P.ntypes * P.ntypes;
-        for (int k = tid; k < nn; k += kTileThreads) sm.mat[k] = P.matrix[k];
+        for (int k = tid; k < nn; k += kT) sm.mat[k] = P.matrix[k];
     }
     const float* M = SMEM_M ? sm.mat : P.matrix;
-    const int s0 = blockIdx.x * kTileTargets;
-    const int nvalid = min(kTileTargets, P.n - s0);
+    const int s0 = blockIdx.x * kT;
+    const int nvalid = min(kT, P.n - s0);
     const bool valid = tid < nvalid;
     const int s = s0 + tid;
     float4 me = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -658,7 +737,7 @@ __global__ void __launch_bounds__(kTileThreads) k_force_tile(const ForceArgs<D> 
     if (start) sm.seg[before + __popc(bal & ((1u << (tid & 31)) - 1u))] = tid;
     if (tid == 0) {
         int t = 0;
-        for (int w = 0; w < kTileTargets / 32; ++w) t += sm.wsum[w];
+        for (int w = 0; w < kT / 32; ++w) t += sm.wsum[w];
         sm.nseg = t;
         sm.seg[t] = nvalid;
     }
@@ -683,10 +762,14 @@ __global__ void __launch_bounds__(kTileThreads) k_force_tile(const ForceArgs<D> 
                 const int self_j = sm.coff[own] + (s - sm.cglob[own]);
                 const int cy = D == 3 ? srow % nx : srow, cz = D == 3 ? srow / nx : 0;
                 const bool shift = P.wrap && (cxb == nx - 1 || cy == nx - 1 || (D == 3 && cz == nx - 1));
-                if (shift)
-                    defer = tile_run<D, DBG, true>(A, sm, Mrow, ncell, j0, j1, self_j, px, py, pz, acc);
-                else
-                    defer = tile_run<D, DBG, false>(A, sm, Mrow, ncell, j0, j1, self_j, px, py, pz, acc);
+                // The target itself splits its run: [j0, self_j) and (self_j, j1).
+                if (shift) {
+                    defer = tile_range<D, DBG, true>(A, sm, Mrow, ncell, j0, self_j, px, py, pz, acc);
+                    defer |= tile_range<D, DBG, true>(A, sm, Mrow, ncell, self_j + 1, j1, px, py, pz, acc);
+                } else {
+                    defer = tile_range<D, DBG, false>(A, sm, Mrow, ncell, j0, self_j, px, py, pz, acc);
+                    defer |= tile_range<D, DBG, false>(A, sm, Mrow, ncell, self_j + 1, j1, px, py, pz, acc);
+                }
             } else {
                 defer = true;
             }
@@ -701,62 +784,28 @@ __global__ void __launch_bounds__(kTileThreads) k_force_tile(const ForceArgs<D> 
         A.rank[s] = bin_count(A.counts, newcell, mask);
         A.cell[s] = newcell;
     }
-    defer_targets(A.defer_count, A.defer_list, valid && defer, s);
-}
-
-// Sum of `v` over the warp in a fixed butterfly order (the same bits on
-// every run); every lane receives the total.
-__device__ __forceinline__ float warp_sum(float v) {
-#pragma unroll
-    for (int d = 16; d > 0; d >>= 1) v += __shfl_xor_sync(kFull, v, d);
-    return v;
-}
-
-// Deferred targets, one warp each: the lanes split the candidates of the
-// global-memory stencil (with the FP64 decisions), their partial sums are
-// combined by warp_sum, and lane 0 runs the epilogue.
-template <int D, bool DBG, bool SMEM_M>
-__global__ void __launch_bounds__(kThreads) k_force_fixup(const __grid_constant__ ForceArgs<D> A) {
-    const ForceParams& P = A.p;
-    __shared__ float smat[kSmemMatrixMax * kSmemMatrixMax];
-    const float* M = P.matrix;
-    if (SMEM_M) {
-        const int nn = P.ntypes * P.ntypes;
-        for (int k = threadIdx.x; k < nn; k += kThreads) smat[k] = P.matrix[k];
-        __syncthreads();
-        M = smat;
+    // Deferred targets of this block (FP64 band pairs, overfull segments),
+    // one warp each, from global memory.  Most blocks have none.
+    const int warp = tid >> 5, lane = tid & 31;
+    const unsigned dm = __ballot_sync(kFull, valid && defer);
+    __syncthreads();  // rowid and wsum are free again
+    if (lane == 0) sm.wsum[warp] = __popc(dm);
+    __syncthreads();
+    int nd = 0, dbefore = 0;
+    for (int w = 0; w < kT / 32; ++w) {
+        const int x = sm.wsum[w];
+        dbefore += w < warp ? x : 0;
+        nd += x;
     }
-    const int lane = threadIdx.x & 31;
-    const int warps = gridDim.x * (kThreads / 32);
-    const int count = (int)*(volatile const uint32_t*)A.defer_count;
-    for (int w = blockIdx.x * (kThreads / 32) + (threadIdx.x >> 5); w < count; w += warps) {
-        const int s = (int)A.defer_list[w];
-        const float4 me = A.bpt[s];
-        const float px = me.x, py = me.y, pz = D == 3 ? me.z : 0.f;
-        Acc acc = stencil_scan<D, DBG>(A, M + Layout<D>::type(me) * P.ntypes, s, px, py, pz,
-                                       sliver_mask<D>(P, px, py, pz), lane, 32);
-        acc.x = warp_sum(acc.x);
-        acc.y = warp_sum(acc.y);
-        if (D == 3) acc.z = warp_sum(acc.z);
-        if (DBG) {
-#pragma unroll
-            for (int d = 16; d > 0; d >>= 1) {
-                acc.pairs += __shfl_xor_sync(kFull, acc.pairs, d);
-                acc.hs += __shfl_xor_sync(kFull, acc.hs, d);
-                acc.hx ^= __shfl_xor_sync(kFull, acc.hx, d);
-                acc.cand += __shfl_xor_sync(kFull, acc.cand, d);
-            }
-        }
-        if (lane == 0) {
-            const uint32_t newcell = integrate<D, DBG>(A, s, me, acc);
-            A.rank[s] = atomicAdd(A.counts + newcell, 1u);
-            A.cell[s] = newcell;
-        }
-    }
+    if (nd == 0) return;  // block-uniform
+    if (valid && defer) sm.rowid[dbefore + __popc(dm & ((1u << lane) - 1u))] = s;
+    if (tid == 0) atomicAdd(A.defer_count, (uint32_t)nd);
+    __syncthreads();
+    for (int d = warp; d < nd; d += kT / 32) fixup_target<D, DBG>(A, M, sm.rowid[d], lane);
 }
 
 template <int D, bool DBG>
-void launch_variant(cudaStream_t st, const ForceArgs<D>& A, bool general, int fixup_blocks) {
+void launch_variant(cudaStream_t st, const ForceArgs<D>& A, bool general) {
     const int n = A.p.n;
     const bool smem = A.p.ntypes <= kSmemMatrixMax;
     if (general) {
@@ -766,18 +815,14 @@ void launch_variant(cudaStream_t st, const ForceArgs<D>& A, bool general, int fi
             k_force_general<D, DBG, true><<<grid, kThreads, sb, st>>>(A);
         else
             k_force_general<D, DBG, false><<<grid, kThreads, 0, st>>>(A);
-    } else if (fixup_blocks == 0) {
-        const int grid = (n + kTileTargets - 1) / kTileTargets;
+    } else {
+        constexpr int kT = TileCfg<D>::kTargets;
+        const int grid = (n + kT - 1) / kT;
         const size_t sb = sizeof(TileSmem<D>);
         if (smem)
-            k_force_tile<D, DBG, true><<<grid, kTileThreads, sb, st>>>(A);
+            k_force_tile<D, DBG, true><<<grid, kT, sb, st>>>(A);
         else
-            k_force_tile<D, DBG, false><<<grid, kTileThreads, sb, st>>>(A);
-    } else {
-        if (smem)
-            k_force_fixup<D, DBG, true><<<fixup_blocks, kThreads, 0, st>>>(A);
-        else
-            k_force_fixup<D, DBG, false><<<fixup_blocks, kThreads, 0, st>>>(A);
+            k_force_tile<D, DBG, false><<<grid, kT, sb, st>>>(A);
     }
 }
 
@@ -795,7 +840,6 @@ ForceArgs<D> make_args(const ForceParams& p, StateBuf<D> b, const uint32_t* csta
     A.rank = rank;
     A.counts = counts;
     A.defer_count = defer;
-    A.defer_list = defer + 1;
     A.dbg = dbg ? *dbg : DebugOut{nullptr, nullptr, nullptr, nullptr, nullptr};
     return A;
 }
@@ -809,33 +853,15 @@ void launch_force(cudaStream_t st, const ForceParams& p, bool general, StateBuf<
     if (p.n <= 0) return;
     const ForceArgs<D> A = make_args<D>(p, b, cstart, a, cell, rank, counts, defer, dbg);
     if (dbg)
-        launch_variant<D, true>(st, A, general, 0);
+        launch_variant<D, true>(st, A, general);
     else
-        launch_variant<D, false>(st, A, general, 0);
-}
-
-template <int D>
-void launch_force_fixup(cudaStream_t st, const ForceParams& p, bool general, StateBuf<D> b, const uint32_t* cstart,
-                        StateBuf<D> a, uint32_t* cell, uint32_t* rank, uint32_t* counts, uint32_t* defer,
-                        const DebugOut* dbg, int blocks) {
-    if (p.n <= 0 || general) return;
-    const ForceArgs<D> A = make_args<D>(p, b, cstart, a, cell, rank, counts, defer, dbg);
-    if (dbg)
-        launch_variant<D, true>(st, A, false, blocks);
-    else
-        launch_variant<D, false>(st, A, false, blocks);
+        launch_variant<D, false>(st, A, general);
 }
 
 template void launch_force<2>(cudaStream_t, const ForceParams&, bool, StateBuf<2>, const uint32_t*, StateBuf<2>,
                               uint32_t*, uint32_t*, uint32_t*, uint32_t*, const DebugOut*);
 template void launch_force<3>(cudaStream_t, const ForceParams&, bool, StateBuf<3>, const uint32_t*, StateBuf<3>,
                               uint32_t*, uint32_t*, uint32_t*, uint32_t*, const DebugOut*);
-template void launch_force_fixup<2>(cudaStream_t, const ForceParams&, bool, StateBuf<2>, const uint32_t*,
-                                    StateBuf<2>, uint32_t*, uint32_t*, uint32_t*, uint32_t*, const DebugOut*,
-                                    int);
-template void launch_force_fixup<3>(cudaStream_t, const ForceParams&, bool, StateBuf<3>, const uint32_t*,
-                                    StateBuf<3>, uint32_t*, uint32_t*, uint32_t*, uint32_t*, const DebugOut*,
-                                    int);
 
 template <int D>
 cudaError_t allow_tile_smem() {

@@ -157,24 +157,20 @@ int scan_blocks(int ncells);
 // set to 0 (the step's deferred-target count) when not null.
 void launch_scan(cudaStream_t st, uint32_t* counts, int ncells, uint32_t* cstart, unsigned long long* state,
                  uint32_t* status, uint32_t* zero_word);
+// slot_cell (may be null): receives the cell of each sorted slot.
 void launch_scatter(cudaStream_t st, int n, const uint32_t* cell, const uint32_t* rank, const uint32_t* cstart,
-                    uint32_t* perm);
+                    uint32_t* perm, uint32_t* slot_cell = nullptr);
 
 template <int D>
-void launch_gather(cudaStream_t st, int n, const uint32_t* perm, const uint32_t* cell, const uint32_t* cstart,
+void launch_gather(cudaStream_t st, int n, const uint32_t* perm, const uint32_t* slot_cell, const uint32_t* cstart,
                    StateBuf<D> a, StateBuf<D> b, int32_t* cell_sorted);
 
-// `defer`: 1 + n words, word 0 zeroed before the step (deferred-target list).
+// `defer`: one word, zeroed before the step; counts the targets the tiled
+// kernel recomputed in its deferred pass.
 template <int D>
 void launch_force(cudaStream_t st, const ForceParams& p, bool general, StateBuf<D> b, const uint32_t* cstart,
                   StateBuf<D> a, uint32_t* cell, uint32_t* rank, uint32_t* counts, uint32_t* defer,
                   const DebugOut* dbg);
-
-// Completes the targets k_force_tile deferred (no-op for nx < 3).
-template <int D>
-void launch_force_fixup(cudaStream_t st, const ForceParams& p, bool general, StateBuf<D> b, const uint32_t* cstart,
-                        StateBuf<D> a, uint32_t* cell, uint32_t* rank, uint32_t* counts, uint32_t* defer,
-                        const DebugOut* dbg, int blocks);
 
 // Opts the tiled force kernel in to its dynamic shared memory (> 48 KB) on
 // the current device; called once per context.

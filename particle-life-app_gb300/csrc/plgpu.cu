@@ -31,7 +31,7 @@ constexpr int kMaxAxisCells = 1 << 20;
 constexpr int kMaxTypes = 1024;
 constexpr double kBandRel = 1.0 / (1 << 19);  // FP32 decision band: 2^-19 relative
 
-const char* kKernelNames[PLG_K_COUNT] = {"scan", "scatter", "gather", "force", "fixup"};
+const char* kKernelNames[PLG_K_COUNT] = {"scan", "scatter", "gather", "force"};
 
 // Staging layout for host <-> device copies: pos[3n] vel[3n] (double), type[n] id[n] (int32).
 size_t stage_bytes(int64_t cap) { return (size_t)cap * (3 * 8 + 3 * 8 + 4 + 4); }
@@ -78,8 +78,8 @@ struct plg_ctx {
     uint32_t* cell = nullptr;
     uint32_t* rank = nullptr;
     uint32_t* perm = nullptr;
-    uint32_t* defer = nullptr;  // deferred-target count + list (force -> fixup)
-    int fixup_blocks = 0;
+    uint32_t* slot_cell = nullptr;  // cell of each sorted slot (scatter -> gather)
+    uint32_t* defer = nullptr;  // targets the force kernel deferred in the last step
     unsigned char* stage = nullptr;
 
     uint32_t* status_d = nullptr;
@@ -249,19 +249,15 @@ void enqueue_body(plg_ctx* c, const DebugOut* dbg, int32_t* cell_sorted) {
     launch_scan(st, c->counts, c->ncells, c->cstart, c->scan_state, c->status_d, c->general ? nullptr : c->defer);
     k1(PLG_K_SCAN);
     k0(PLG_K_SCATTER);
-    launch_scatter(st, n, c->cell, c->rank, c->cstart, c->perm);
+    launch_scatter(st, n, c->cell, c->rank, c->cstart, c->perm, c->slot_cell);
     k1(PLG_K_SCATTER);
     k0(PLG_K_GATHER);
-    launch_gather<D>(st, n, c->perm, c->cell, c->cstart, buf_a<D>(c), buf_b<D>(c), cell_sorted);
+    launch_gather<D>(st, n, c->perm, c->slot_cell, c->cstart, buf_a<D>(c), buf_b<D>(c), cell_sorted);
     k1(PLG_K_GATHER);
     k0(PLG_K_FORCE);
     launch_force<D>(st, c->fp, c->general, buf_b<D>(c), c->cstart, buf_a<D>(c), c->cell, c->rank, c->counts,
                     c->defer, dbg);
     k1(PLG_K_FORCE);
-    k0(PLG_K_FIXUP);
-    launch_force_fixup<D>(st, c->fp, c->general, buf_b<D>(c), c->cstart, buf_a<D>(c), c->cell, c->rank, c->counts,
-                          c->defer, dbg, c->fixup_blocks);
-    k1(PLG_K_FIXUP);
 }
 
 void enqueue_body_dim(plg_ctx* c, const DebugOut* dbg, int32_t* cell_sorted) {
@@ -368,9 +364,10 @@ int read_status(plg_ctx* c) {
 
 int free_all(plg_ctx* c) {
     destroy_graph(c);
-    void* ptrs[] = {c->bounds, c->counts, c->cstart, c->scan_state, c->matrix, c->apt, c->bpt, c->avel, c->bvel,
-                    c->cell, c->rank, c->perm, c->defer, c->stage, c->status_d, c->dbg_pairs, c->dbg_hsum, c->dbg_hxor,
-                    c->dbg_cand, c->dbg_acc, c->dbg_cell};
+    void* ptrs[] = {c->bounds,    c->counts,   c->cstart,   c->scan_state, c->matrix,   c->apt,
+                    c->bpt,       c->avel,     c->bvel,     c->cell,       c->rank,     c->perm,
+                    c->slot_cell, c->defer,    c->stage,    c->status_d,   c->dbg_pairs, c->dbg_hsum,
+                    c->dbg_hxor,  c->dbg_cand, c->dbg_acc,  c->dbg_cell};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (c->status_h) cudaFreeHost(c->status_h);
@@ -462,12 +459,7 @@ int plg_create(int dim, int64_t capacity, plg_ctx** out) {
     const size_t cap = (size_t)capacity;
     e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) rc = PLG_E_CUDA;
-    int sms = 0;
-    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device) != cudaSuccess) rc = PLG_E_CUDA;
     if (!rc && force_kernels_init() != cudaSuccess) rc = PLG_E_CUDA;
-    // Deferred targets are rare (FP64 band pairs, overfull segments): one
-    // wave of 256-thread blocks, capped by the capacity.
-    c->fixup_blocks = (int)std::min<int64_t>(2 * (int64_t)sms, (capacity + 255) / 256);
     dmalloc((void**)&c->apt, sizeof(float4) * cap);
     dmalloc((void**)&c->bpt, sizeof(float4) * cap);
     dmalloc(&c->avel, vel_sz * cap);
@@ -475,7 +467,8 @@ int plg_create(int dim, int64_t capacity, plg_ctx** out) {
     dmalloc((void**)&c->cell, sizeof(uint32_t) * cap);
     dmalloc((void**)&c->rank, sizeof(uint32_t) * cap);
     dmalloc((void**)&c->perm, sizeof(uint32_t) * cap);
-    dmalloc((void**)&c->defer, sizeof(uint32_t) * (cap + 1));
+    dmalloc((void**)&c->slot_cell, sizeof(uint32_t) * cap);
+    dmalloc((void**)&c->defer, sizeof(uint32_t));
     dmalloc((void**)&c->stage, stage_bytes(capacity));
     dmalloc((void**)&c->status_d, 64);
     if (!rc && cudaMallocHost((void**)&c->status_h, 64) != cudaSuccess) rc = PLG_E_NO_MEMORY;

@@ -28,7 +28,7 @@ PLG_ACCEL_PARTICLE_LIFE = 1
 PLG_NOALLOC_MAX_PARTICLES = 1 << 18
 PLG_NOALLOC_MAX_CELLS = 1 << 18
 
-KERNELS = ["scan", "scatter", "gather", "force", "fixup"]
+KERNELS = ["scan", "scatter", "gather", "force"]
 
 
 class plg_settings(C.Structure):

@@ -314,7 +314,7 @@ class GpuWorld:
         return dict(cell=cell, pairs=pairs, hsum=hs, hxor=hx, acc=acc, candidates=cand.value)
 
     def deferred(self) -> int:
-        """Targets of the last step handled by the global-memory fixup kernel."""
+        """Targets of the last step the force kernel recomputed in its deferred (global-memory) pass."""
         v = _lib.C.c_int64()
         self._c(self.lib.plg_step_stats(self.ctx, _lib.C.byref(v)), "plg_step_stats")
         return v.value
