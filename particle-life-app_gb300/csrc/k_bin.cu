@@ -29,22 +29,58 @@ inline int blocks_for(int n, int threads) { return (n + threads - 1) / threads; 
 
 // ---- upload: host double layout -> FP32 SoA, validation, first binning ----
 
+// The host arrays may be page-locked host memory read in place over the host
+// link, so each block moves its particles' interleaved doubles through shared
+// memory with warp-contiguous 16-byte accesses (`vec`: the array bases are
+// 16-byte aligned; block offsets are multiples of 256 * 24 bytes).
+__device__ __forceinline__ void block_copy_in(double* __restrict__ dst, const double* __restrict__ src, int cnt,
+                                              bool vec) {
+    if (vec) {
+        const int c2 = cnt >> 1;
+        for (int k = threadIdx.x; k < c2; k += kThreads)
+            reinterpret_cast<double2*>(dst)[k] = reinterpret_cast<const double2*>(src)[k];
+        if ((cnt & 1) && threadIdx.x == 0) dst[cnt - 1] = src[cnt - 1];
+    } else {
+        for (int k = threadIdx.x; k < cnt; k += kThreads) dst[k] = src[k];
+    }
+}
+
+__device__ __forceinline__ void block_copy_out(double* __restrict__ dst, const double* __restrict__ src, int cnt,
+                                               bool vec) {
+    if (vec) {
+        const int c2 = cnt >> 1;
+        for (int k = threadIdx.x; k < c2; k += kThreads)
+            reinterpret_cast<double2*>(dst)[k] = reinterpret_cast<const double2*>(src)[k];
+        if ((cnt & 1) && threadIdx.x == 0) dst[cnt - 1] = src[cnt - 1];
+    } else {
+        for (int k = threadIdx.x; k < cnt; k += kThreads) dst[k] = src[k];
+    }
+}
+
 template <int D>
 __global__ void __launch_bounds__(kThreads) k_upload(int n, const double* __restrict__ pos,
                                                      const double* __restrict__ vel,
                                                      const int32_t* __restrict__ type, int ntypes,
                                                      StateBuf<D> a, uint32_t* __restrict__ cell,
                                                      uint32_t* __restrict__ rank, uint32_t* counts, Grid g,
-                                                     uint32_t* status) {
-    const int i = blockIdx.x * kThreads + threadIdx.x;
-    const bool valid = i < n;
+                                                     uint32_t* status, bool vec) {
+    __shared__ __align__(16) double sp[3 * kThreads];
+    __shared__ __align__(16) double sv[3 * kThreads];
+    const int i0 = blockIdx.x * kThreads;
+    const int m = min(kThreads, n - i0);
+    block_copy_in(sp, pos + 3 * (size_t)i0, 3 * m, vec);
+    if (vel) block_copy_in(sv, vel + 3 * (size_t)i0, 3 * m, vec);
+    __syncthreads();
+    const int t = threadIdx.x;
+    const int i = i0 + t;
+    const bool valid = t < m;
     uint32_t c = 0;
     uint32_t bad = 0;
     if (valid) {
         float p[3];
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
-            double x = pos[3 * (size_t)i + k];
+            double x = sp[3 * t + k];
             if (k < D && !(x >= 0.0 && x <= 1.0)) {  // also rejects NaN
                 bad |= kDevBadPosition;
                 x = 0.0;
@@ -55,7 +91,7 @@ __global__ void __launch_bounds__(kThreads) k_upload(int n, const double* __rest
         if (vel) {
 #pragma unroll
             for (int k = 0; k < D; ++k) {
-                double x = vel[3 * (size_t)i + k];
+                double x = sv[3 * t + k];
                 if (!isfinite(x)) {
                     bad |= kDevBadVelocity;
                     x = 0.0;
@@ -63,16 +99,16 @@ __global__ void __launch_bounds__(kThreads) k_upload(int n, const double* __rest
                 v[k] = __double2float_rn(x);
             }
         }
-        int t = type[i];
-        if (t < 0 || t >= ntypes) {
+        int ty = type[i];
+        if (ty < 0 || ty >= ntypes) {
             bad |= kDevBadType;
-            t = 0;
+            ty = 0;
         }
         if constexpr (D == 2) {
-            a.pt[i] = make_float4(p[0], p[1], __int_as_float(t), __int_as_float(i));
+            a.pt[i] = make_float4(p[0], p[1], __int_as_float(ty), __int_as_float(i));
             reinterpret_cast<float2*>(a.vel)[i] = make_float2(v[0], v[1]);
         } else {
-            a.pt[i] = make_float4(p[0], p[1], p[2], __int_as_float(t));
+            a.pt[i] = make_float4(p[0], p[1], p[2], __int_as_float(ty));
             reinterpret_cast<float4*>(a.vel)[i] = make_float4(v[0], v[1], v[2], __int_as_float(i));
         }
         c = cell_index<D>(p[0], p[1], p[2], g);
@@ -105,30 +141,38 @@ __global__ void __launch_bounds__(kThreads) k_rebin(int n, StateBuf<D> a, uint32
 
 // ---- download: FP32 SoA -> PhysicsSnapshot layout (app/PhysicsSnapshot.java:50-58) ----
 
+// Like the upload, the interleaved doubles leave through shared memory with
+// warp-contiguous 16-byte stores (the destination may be page-locked host
+// memory written in place).
 template <int D>
 __global__ void __launch_bounds__(kThreads) k_download(int n, StateBuf<D> a, double* __restrict__ pos,
                                                        double* __restrict__ vel, int32_t* __restrict__ type,
-                                                       int32_t* __restrict__ id) {
-    const int i = blockIdx.x * kThreads + threadIdx.x;
-    if (i >= n) return;
-    const float4 p = a.pt[i];
-    const typename Layout<D>::Vel v = a.vel[i];
-    if (pos) {
-        pos[3 * (size_t)i + 0] = p.x;
-        pos[3 * (size_t)i + 1] = p.y;
-        pos[3 * (size_t)i + 2] = D == 3 ? p.z : 0.0;
-    }
-    if (vel) {
-        vel[3 * (size_t)i + 0] = v.x;
-        vel[3 * (size_t)i + 1] = v.y;
+                                                       int32_t* __restrict__ id, bool vec) {
+    __shared__ __align__(16) double sp[3 * kThreads];
+    __shared__ __align__(16) double sv[3 * kThreads];
+    const int i0 = blockIdx.x * kThreads;
+    const int m = min(kThreads, n - i0);
+    const int t = threadIdx.x;
+    const int i = i0 + t;
+    if (t < m) {
+        const float4 p = a.pt[i];
+        const typename Layout<D>::Vel v = a.vel[i];
+        sp[3 * t + 0] = p.x;
+        sp[3 * t + 1] = p.y;
+        sp[3 * t + 2] = D == 3 ? p.z : 0.0;
+        sv[3 * t + 0] = v.x;
+        sv[3 * t + 1] = v.y;
         if constexpr (D == 3) {
-            vel[3 * (size_t)i + 2] = v.z;
+            sv[3 * t + 2] = v.z;
         } else {
-            vel[3 * (size_t)i + 2] = 0.0;
+            sv[3 * t + 2] = 0.0;
         }
+        if (type) type[i] = Layout<D>::type(p);
+        if (id) id[i] = Layout<D>::id(p, v);
     }
-    if (type) type[i] = Layout<D>::type(p);
-    if (id) id[i] = Layout<D>::id(p, v);
+    __syncthreads();
+    if (pos) block_copy_out(pos + 3 * (size_t)i0, sp, 3 * m, vec);
+    if (vel) block_copy_out(vel + 3 * (size_t)i0, sv, 3 * m, vec);
 }
 
 // ---- block scan helpers ----
@@ -304,12 +348,15 @@ __global__ void __launch_bounds__(kThreads) k_gather(int n, const uint32_t* __re
 
 }  // namespace
 
+inline bool aligned16(const void* p) { return ((uintptr_t)p & 15u) == 0; }
+
 template <int D>
 void launch_upload(cudaStream_t st, int n, const double* pos, const double* vel, const int32_t* type, int ntypes,
                    StateBuf<D> a, uint32_t* cell, uint32_t* rank, uint32_t* counts, Grid g, uint32_t* status) {
     if (n <= 0) return;
+    const bool vec = aligned16(pos) && aligned16(vel);
     k_upload<D><<<blocks_for(n, kThreads), kThreads, 0, st>>>(n, pos, vel, type, ntypes, a, cell, rank, counts, g,
-                                                              status);
+                                                              status, vec);
 }
 
 template <int D>
@@ -321,7 +368,8 @@ void launch_rebin(cudaStream_t st, int n, StateBuf<D> a, uint32_t* cell, uint32_
 template <int D>
 void launch_download(cudaStream_t st, int n, StateBuf<D> a, double* pos, double* vel, int32_t* type, int32_t* id) {
     if (n <= 0) return;
-    k_download<D><<<blocks_for(n, kThreads), kThreads, 0, st>>>(n, a, pos, vel, type, id);
+    const bool vec = aligned16(pos) && aligned16(vel);
+    k_download<D><<<blocks_for(n, kThreads), kThreads, 0, st>>>(n, a, pos, vel, type, id, vec);
 }
 
 int scan_blocks(int ncells) { return blocks_for(ncells, kScanTile); }

@@ -34,7 +34,26 @@ constexpr double kBandRel = 1.0 / (1 << 19);  // FP32 decision band: 2^-19 relat
 const char* kKernelNames[PLG_K_COUNT] = {"scan", "scatter", "gather", "force"};
 
 // Staging layout for host <-> device copies: pos[3n] vel[3n] (double), type[n] id[n] (int32).
-size_t stage_bytes(int64_t cap) { return (size_t)cap * (3 * 8 + 3 * 8 + 4 + 4); }
+// Staging rows are padded to an even particle count so that every array
+// starts on a 16-byte boundary (the conversion kernels use 16-byte accesses).
+size_t stage_rows(int64_t cap) { return ((size_t)cap + 1) & ~(size_t)1; }
+size_t stage_bytes(int64_t cap) { return stage_rows(cap) * (3 * 8 + 3 * 8 + 4 + 4); }
+
+// Device address of a page-locked host buffer (cudaHostAlloc / cudaMallocHost
+// / cudaHostRegister), or null for pageable memory.  The conversion kernels
+// read and write page-locked buffers in place over the host link instead of
+// staging them through device memory with separate copies.
+template <typename T>
+T* host_mapped(T* p) {
+    if (!p) return nullptr;
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (a.type != cudaMemoryTypeHost || !a.devicePointer) return nullptr;
+    return static_cast<T*>(a.devicePointer);
+}
 
 }  // namespace
 
@@ -575,13 +594,26 @@ int plg_upload(plg_ctx* c, int64_t n, const double* pos, const double* vel, cons
     DeviceGuard g(c->device);
     cudaStream_t st = c->stream;
     double* dpos = (double*)c->stage;
-    double* dvel = dpos + 3 * (size_t)c->cap;
-    int32_t* dtype = (int32_t*)(dvel + 3 * (size_t)c->cap);
+    double* dvel = dpos + 3 * stage_rows(c->cap);
+    int32_t* dtype = (int32_t*)(dvel + 3 * stage_rows(c->cap));
     c->state_valid = false;
     if (n > 0) {
-        CK(c, cudaMemcpyAsync(dpos, pos, sizeof(double) * 3 * (size_t)n, cudaMemcpyHostToDevice, st));
-        if (vel) CK(c, cudaMemcpyAsync(dvel, vel, sizeof(double) * 3 * (size_t)n, cudaMemcpyHostToDevice, st));
-        CK(c, cudaMemcpyAsync(dtype, type, sizeof(int32_t) * (size_t)n, cudaMemcpyHostToDevice, st));
+        // Page-locked arrays are read in place by the upload kernel.
+        const double* mpos = host_mapped(pos);
+        const double* mvel = host_mapped(vel);
+        const int32_t* mtype = host_mapped(type);
+        if (mpos)
+            dpos = const_cast<double*>(mpos);
+        else
+            CK(c, cudaMemcpyAsync(dpos, pos, sizeof(double) * 3 * (size_t)n, cudaMemcpyHostToDevice, st));
+        if (mvel)
+            dvel = const_cast<double*>(mvel);
+        else if (vel)
+            CK(c, cudaMemcpyAsync(dvel, vel, sizeof(double) * 3 * (size_t)n, cudaMemcpyHostToDevice, st));
+        if (mtype)
+            dtype = const_cast<int32_t*>(mtype);
+        else
+            CK(c, cudaMemcpyAsync(dtype, type, sizeof(int32_t) * (size_t)n, cudaMemcpyHostToDevice, st));
     }
     CK(c, cudaMemsetAsync(c->counts, 0, sizeof(uint32_t) * (size_t)c->ncells, st));
     CK(c, cudaMemsetAsync(c->status_d, 0, sizeof(uint32_t), st));
@@ -649,21 +681,29 @@ int plg_download(plg_ctx* c, double* pos, double* vel, int32_t* type, int32_t* i
     cudaStream_t st = c->stream;
     const size_t n = (size_t)c->n;
     double* dpos = (double*)c->stage;
-    double* dvel = dpos + 3 * (size_t)c->cap;
-    int32_t* dtype = (int32_t*)(dvel + 3 * (size_t)c->cap);
-    int32_t* did = dtype + (size_t)c->cap;
+    double* dvel = dpos + 3 * stage_rows(c->cap);
+    int32_t* dtype = (int32_t*)(dvel + 3 * stage_rows(c->cap));
+    int32_t* did = dtype + stage_rows(c->cap);
     if (n > 0) {
+        // Page-locked arrays are written in place by the download kernel;
+        // the others go through the staging buffer and a copy.
+        double* mpos = host_mapped(pos);
+        double* mvel = host_mapped(vel);
+        int32_t* mtype = host_mapped(type);
+        int32_t* mid = host_mapped(id);
+        double* kpos = pos ? (mpos ? mpos : dpos) : nullptr;
+        double* kvel = vel ? (mvel ? mvel : dvel) : nullptr;
+        int32_t* ktype = type ? (mtype ? mtype : dtype) : nullptr;
+        int32_t* kid = id ? (mid ? mid : did) : nullptr;
         if (c->dim == 2)
-            launch_download<2>(st, (int)n, buf_a<2>(c), pos ? dpos : nullptr, vel ? dvel : nullptr,
-                               type ? dtype : nullptr, id ? did : nullptr);
+            launch_download<2>(st, (int)n, buf_a<2>(c), kpos, kvel, ktype, kid);
         else
-            launch_download<3>(st, (int)n, buf_a<3>(c), pos ? dpos : nullptr, vel ? dvel : nullptr,
-                               type ? dtype : nullptr, id ? did : nullptr);
+            launch_download<3>(st, (int)n, buf_a<3>(c), kpos, kvel, ktype, kid);
         CK(c, cudaGetLastError());
-        if (pos) CK(c, cudaMemcpyAsync(pos, dpos, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, st));
-        if (vel) CK(c, cudaMemcpyAsync(vel, dvel, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, st));
-        if (type) CK(c, cudaMemcpyAsync(type, dtype, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, st));
-        if (id) CK(c, cudaMemcpyAsync(id, did, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, st));
+        if (pos && !mpos) CK(c, cudaMemcpyAsync(pos, dpos, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, st));
+        if (vel && !mvel) CK(c, cudaMemcpyAsync(vel, dvel, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, st));
+        if (type && !mtype) CK(c, cudaMemcpyAsync(type, dtype, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, st));
+        if (id && !mid) CK(c, cudaMemcpyAsync(id, did, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, st));
     }
     CK(c, cudaStreamSynchronize(st));
     return PLG_OK;
