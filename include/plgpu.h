@@ -196,6 +196,63 @@ int plg_step_stats(plg_ctx* ctx, int64_t* deferred);
  * TFLOP/s (an FFMA counts 2 flops).  Runs for about 0.1 s. */
 int plg_probe_fp32_peak(double* tflops);
 
+/* ---- batched worlds ---------------------------------------------------- */
+
+/* Many independent worlds advanced together: one step launch sorts and
+ * steps every world (no counterpart in the reference, which runs one
+ * Physics at a time; each world computes exactly what plg_step computes for
+ * it).  All worlds of a batch have the same dimension and at least 3 cells
+ * per axis (rmax <= 1/3).  One thread drives a batch. */
+typedef struct plg_batch plg_batch;
+
+/* One world: settings (plg_set_settings), matrix (plg_set_matrix) and its
+ * initial particles (plg_upload layouts).  Host buffers are read during the
+ * call only; page-locked buffers are read in place. */
+typedef struct plg_world_desc {
+    plg_settings settings;
+    int32_t ntypes;          /* matrix size, 1..1024 (<= 16: matrix in shared memory) */
+    const double* matrix;    /* ntypes x ntypes, row-major */
+    int64_t n;               /* particles */
+    const double* pos;       /* double[3n], each coordinate in [0,1] */
+    const double* vel;       /* double[3n] or NULL */
+    const int32_t* type;     /* int32[n], 0 <= type < ntypes */
+} plg_world_desc;
+
+/* Capacities: particles, worlds (<= 1024) and cells over all worlds. */
+int plg_batch_create(int32_t dim, int64_t particle_capacity, int32_t world_capacity,
+                     int64_t cell_capacity, plg_batch** out);
+int plg_batch_destroy(plg_batch* batch);
+
+/* Removes `nremove` worlds and adds `nadd`, then lays the batch out again
+ * (one pass over all particles); ids_out[k] receives the id of add[k].
+ * Everything is checked before anything changes: PLG_E_CAPACITY,
+ * PLG_E_INVALID_ARG (unknown id, bad description), PLG_E_UNSUPPORTED
+ * (rmax > 1/3, accelerator kind). */
+int plg_batch_update(plg_batch* batch, int32_t nremove, const int32_t* remove_ids,
+                     int32_t nadd, const plg_world_desc* add, int32_t* ids_out);
+
+/* nsteps x Physics.update() for every world; the blocking form waits. */
+int plg_batch_step(plg_batch* batch, int32_t nsteps);
+int plg_batch_step_async(plg_batch* batch, int32_t nsteps);
+int plg_batch_sync(plg_batch* batch, double timeout_s);
+
+/* One world's state in its cell-sorted order, like plg_download. */
+int plg_batch_download(plg_batch* batch, int32_t id, double* pos, double* vel,
+                       int32_t* type, int32_t* pid);
+/* A world's particle count, first sorted slot and first global cell. */
+int plg_batch_world_info(plg_batch* batch, int32_t id, int64_t* n, int64_t* first_slot,
+                         int64_t* first_cell);
+int plg_batch_counts(plg_batch* batch, int32_t* nworlds, int64_t* nparticles, int64_t* ncells);
+int plg_batch_set_use_graph(plg_batch* batch, int32_t on);
+int plg_batch_get_stream(plg_batch* batch, void** stream);
+const char* plg_batch_last_error(plg_batch* batch);
+int plg_batch_step_stats(plg_batch* batch, int64_t* deferred);
+/* plg_debug_step over the whole batch: per sorted slot (worlds one after
+ * another), cell = global cell index (world's first cell + its own). */
+int plg_batch_debug_step(plg_batch* batch, int32_t* cell, int32_t* pairs,
+                         uint64_t* hash_sum, uint64_t* hash_xor, float* acc,
+                         int64_t* candidates);
+
 /* ---- cell sort without allocation ------------------------------------- */
 
 /* Capacity of plg_sort_cells_noalloc's fixed device scratch. */

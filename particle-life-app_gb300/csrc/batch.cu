@@ -1,0 +1,695 @@
+// batch.cu — many independent worlds advanced by one step launch.
+//
+// The worlds of a batch share one set of device arrays.  World k owns the
+// sorted slots [p_off, p_off + n) and the global cells [c_off, c_off + nx^D);
+// its bounds table and matrix sit at offsets in shared arrays.  Because the
+// cell ranges are disjoint and ordered by world, one counting sort over the
+// global cell index sorts every world at once and keeps each world's
+// particles contiguous, so a batched step is exactly the single-world graph
+// (scan, scatter, gather, force) over the concatenation, with the force
+// kernel reading each target's world parameters from a device table.  Each
+// world computes exactly what a single-world context computes for it.
+//
+// Membership changes (plg_batch_update) re-lay out the batch in one pass:
+// surviving worlds are copied to their new slots (k_batch_move), new worlds
+// are converted in place from the caller's buffers, and every particle is
+// re-binned with its world's grid.  Their relative particle order is kept,
+// so a world's trajectory does not depend on what else is in the batch.
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "plg_host.h"
+#include "plg_internal.cuh"
+#include "plgpu.h"
+
+using namespace plg;
+
+namespace {
+
+struct WorldRec {
+    int32_t id = 0;
+    int64_t n = 0;
+    int ntypes = 0;
+    plg_settings s{};
+    int nx = 0;
+    int64_t ncells = 0;
+    std::vector<float> bounds;  // nx + 1
+    std::vector<float> matrix;  // ntypes^2
+    int64_t p_off = 0, c_off = 0, m_off = 0, b_off = 0;
+};
+
+}  // namespace
+
+struct plg_batch {
+    int dim = 2;
+    int device = 0;
+    int64_t pcap = 0, ccap = 0;
+    int32_t wcap = 0;
+    cudaStream_t stream = nullptr;
+
+    float4* apt = nullptr;
+    float4* bpt = nullptr;
+    void* avel = nullptr;
+    void* bvel = nullptr;
+    uint32_t* cell = nullptr;
+    uint32_t* rank = nullptr;
+    uint32_t* perm = nullptr;
+    uint32_t* slot_cell = nullptr;
+    uint32_t* counts = nullptr;
+    uint32_t* cstart = nullptr;
+    unsigned long long* scan_state = nullptr;
+    uint32_t* defer = nullptr;
+    uint32_t* status_d = nullptr;
+    uint32_t* status_h = nullptr;
+
+    ForceParams* worlds_d = nullptr;  // wcap
+    int* wp_off_d = nullptr;          // wcap + 1
+    int* move_new_d = nullptr;        // wcap + 1
+    int* move_old_d = nullptr;        // wcap
+    float* bounds_d = nullptr;
+    int64_t bounds_cap = 0;
+    float* matrix_d = nullptr;
+    int64_t matrix_cap = 0;
+    unsigned char* stage = nullptr;  // pageable uploads / downloads
+    int64_t stage_cap = 0;           // bytes
+
+    // instrumented step (allocated on first use)
+    int32_t* dbg_pairs = nullptr;
+    unsigned long long* dbg_hsum = nullptr;
+    unsigned long long* dbg_hxor = nullptr;
+    unsigned long long* dbg_cand = nullptr;
+    float* dbg_acc = nullptr;
+    int32_t* dbg_cell = nullptr;
+
+    std::vector<WorldRec> worlds;  // device order
+    int32_t next_id = 1;
+    int64_t n_total = 0, c_total = 0;
+    bool smem_matrix = true;
+
+    bool use_graph = true;
+    bool graph_dirty = true;
+    cudaGraphExec_t gexec = nullptr;
+    std::string err;
+};
+
+namespace {
+
+constexpr int kMaxBatchWorlds = 1 << 10;  // world index fits the force kernel's segment key
+
+int berr(plg_batch* b, int code, const std::string& msg) {
+    if (b) b->err = msg;
+    return code;
+}
+
+int bcuda(plg_batch* b, const char* what, cudaError_t e) {
+    cudaGetLastError();
+    return berr(b, PLG_E_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define BCK(b, call)                                          \
+    do {                                                      \
+        cudaError_t e_ = (call);                              \
+        if (e_ != cudaSuccess) return bcuda(b, #call, e_);    \
+    } while (0)
+
+struct BatchDeviceGuard {
+    int prev = -1;
+    explicit BatchDeviceGuard(int d) {
+        if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+        if (prev != d) cudaSetDevice(d);
+    }
+    ~BatchDeviceGuard() {
+        int cur = -1;
+        if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
+    }
+};
+
+template <typename T>
+T* mapped_host(T* p) {
+    if (!p) return nullptr;
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (a.type != cudaMemoryTypeHost || !a.devicePointer) return nullptr;
+    return static_cast<T*>(a.devicePointer);
+}
+
+template <typename T>
+int regrow(plg_batch* b, T** p, int64_t* cap, int64_t need, const char* what) {
+    if (*p && *cap >= need) return PLG_OK;
+    BCK(b, cudaStreamSynchronize(b->stream));
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+    *cap = 0;
+    const int64_t want = std::max<int64_t>(need, 1);
+    cudaError_t e = cudaMalloc((void**)p, sizeof(T) * (size_t)want);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        *p = nullptr;
+        return berr(b, PLG_E_NO_MEMORY, std::string("cudaMalloc ") + what + ": " + cudaGetErrorString(e));
+    }
+    *cap = want;
+    return PLG_OK;
+}
+
+size_t batch_stage_bytes(int64_t rows) { return (size_t)rows * (3 * 8 + 3 * 8 + 4 + 4); }
+
+template <int D>
+StateBuf<D> sbuf(float4* pt, void* vel, int64_t off) {
+    return StateBuf<D>{pt + off, (typename Layout<D>::Vel*)vel + off};
+}
+
+void destroy_batch_graph(plg_batch* b) {
+    if (b->gexec) cudaGraphExecDestroy(b->gexec);
+    b->gexec = nullptr;
+    b->graph_dirty = true;
+}
+
+void free_batch(plg_batch* b) {
+    destroy_batch_graph(b);
+    void* ptrs[] = {b->apt,      b->bpt,       b->avel,      b->bvel,        b->cell,     b->rank,
+                    b->perm,     b->slot_cell, b->counts,    b->cstart,      b->scan_state, b->defer,
+                    b->status_d, b->worlds_d,  b->wp_off_d,  b->move_new_d,  b->move_old_d, b->bounds_d,
+                    b->matrix_d, b->stage,     b->dbg_pairs, b->dbg_hsum,    b->dbg_hxor, b->dbg_cand,
+                    b->dbg_acc,  b->dbg_cell};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    if (b->status_h) cudaFreeHost(b->status_h);
+    if (b->stream) cudaStreamDestroy(b->stream);
+}
+
+int find_world(const plg_batch* b, int32_t id) {
+    for (size_t k = 0; k < b->worlds.size(); ++k)
+        if (b->worlds[k].id == id) return (int)k;
+    return -1;
+}
+
+// Host-side checks of one world description (the device path has no CPU
+// fallback, so anything it cannot run is rejected here).
+int check_desc(plg_batch* b, const plg_world_desc& d) {
+    int rc = plg_validate_settings(b->dim, &d.settings);
+    if (rc) return berr(b, rc, "world settings rejected by plg_validate_settings");
+    if (grid_n(d.settings.rmax) < 3)
+        return berr(b, PLG_E_UNSUPPORTED, "batched worlds need rmax <= 1/3 (>= 3 cells per axis)");
+    if (d.ntypes < 1 || d.ntypes > kMaxTypes) return berr(b, PLG_E_INVALID_ARG, "matrix size must be 1..1024");
+    if (!d.matrix) return berr(b, PLG_E_INVALID_ARG, "matrix must not be NULL");
+    for (int64_t k = 0; k < (int64_t)d.ntypes * d.ntypes; ++k)
+        if (!std::isfinite(d.matrix[k])) return berr(b, PLG_E_INVALID_ARG, "matrix entries must be finite");
+    if (d.n < 0) return berr(b, PLG_E_INVALID_ARG, "negative particle count");
+    if (d.n > 0 && (!d.pos || !d.type)) return berr(b, PLG_E_INVALID_ARG, "pos and type must not be NULL");
+    for (int64_t i = 0; i < d.n; ++i) {
+        for (int k = 0; k < b->dim; ++k) {
+            const double x = d.pos[3 * i + k];
+            if (!(x >= 0.0 && x <= 1.0))
+                return berr(b, PLG_E_INVALID_ARG, "positions must lie in [0,1] (ensurePosition first)");
+            if (d.vel && !std::isfinite(d.vel[3 * i + k]))
+                return berr(b, PLG_E_INVALID_ARG, "velocities must be finite");
+        }
+        if (d.type[i] < 0 || d.type[i] >= d.ntypes)
+            return berr(b, PLG_E_INVALID_ARG, "types must lie in [0, matrix size)");
+    }
+    return PLG_OK;
+}
+
+// Writes the device world tables for the current b->worlds layout.
+int upload_tables(plg_batch* b) {
+    const size_t nw = b->worlds.size();
+    int64_t nb = 0, nm = 0;
+    for (const WorldRec& w : b->worlds) {
+        nb += (int64_t)w.bounds.size();
+        nm += (int64_t)w.matrix.size();
+    }
+    int rc;
+    if ((rc = regrow(b, &b->bounds_d, &b->bounds_cap, nb, "bounds"))) return rc;
+    if ((rc = regrow(b, &b->matrix_d, &b->matrix_cap, nm, "matrix"))) return rc;
+    std::vector<float> bounds((size_t)std::max<int64_t>(nb, 1)), matrix((size_t)std::max<int64_t>(nm, 1));
+    std::vector<ForceParams> fp(std::max<size_t>(nw, 1));
+    std::vector<int> off(nw + 1, 0);
+    b->smem_matrix = true;
+    for (size_t k = 0; k < nw; ++k) {
+        const WorldRec& w = b->worlds[k];
+        std::copy(w.bounds.begin(), w.bounds.end(), bounds.begin() + w.b_off);
+        std::copy(w.matrix.begin(), w.matrix.end(), matrix.begin() + w.m_off);
+        ForceParams p{};
+        fill_force_params(w.s, w.nx, w.ncells, w.ntypes, w.bounds[w.nx], p);
+        p.g.bounds = b->bounds_d + w.b_off;
+        p.matrix = b->matrix_d + w.m_off;
+        p.n = (int)w.n;
+        p.cell_base = (uint32_t)w.c_off;
+        p.p_off = (int)w.p_off;
+        fp[k] = p;
+        off[k] = (int)w.p_off;
+        if (w.ntypes > 16) b->smem_matrix = false;
+    }
+    off[nw] = (int)b->n_total;
+    if (nb) BCK(b, cudaMemcpyAsync(b->bounds_d, bounds.data(), sizeof(float) * nb, cudaMemcpyHostToDevice, b->stream));
+    if (nm) BCK(b, cudaMemcpyAsync(b->matrix_d, matrix.data(), sizeof(float) * nm, cudaMemcpyHostToDevice, b->stream));
+    if (nw) BCK(b, cudaMemcpyAsync(b->worlds_d, fp.data(), sizeof(ForceParams) * nw, cudaMemcpyHostToDevice, b->stream));
+    BCK(b, cudaMemcpyAsync(b->wp_off_d, off.data(), sizeof(int) * (nw + 1), cudaMemcpyHostToDevice, b->stream));
+    // The host vectors die at return: wait for the copies.
+    BCK(b, cudaStreamSynchronize(b->stream));
+    return PLG_OK;
+}
+
+template <int D>
+int relayout(plg_batch* b, const std::vector<int>& survivors, const plg_world_desc* add, int32_t nadd,
+             int32_t* ids_out) {
+    destroy_batch_graph(b);  // the step graph refers to the old layout
+    std::vector<WorldRec> next;
+    next.reserve(survivors.size() + (size_t)nadd);
+    std::vector<int> mnew, mold;
+    int64_t p = 0, c = 0, m = 0, bo = 0;
+    for (int k : survivors) {
+        WorldRec w = b->worlds[(size_t)k];
+        mnew.push_back((int)p);
+        mold.push_back((int)w.p_off);
+        w.p_off = p;
+        w.c_off = c;
+        w.m_off = m;
+        w.b_off = bo;
+        p += w.n;
+        c += w.ncells;
+        m += (int64_t)w.matrix.size();
+        bo += (int64_t)w.bounds.size();
+        next.push_back(std::move(w));
+    }
+    const int64_t n_surv = p;
+    mnew.push_back((int)p);
+    for (int32_t a = 0; a < nadd; ++a) {
+        const plg_world_desc& d = add[a];
+        WorldRec w;
+        w.id = b->next_id++;
+        w.n = d.n;
+        w.ntypes = d.ntypes;
+        w.s = d.settings;
+        w.nx = grid_n(d.settings.rmax);
+        w.ncells = (int64_t)w.nx * w.nx * (D == 3 ? w.nx : 1);
+        w.bounds.resize((size_t)w.nx + 1);
+        build_bounds(d.settings.rmax, w.nx, w.bounds.data());
+        w.matrix.resize((size_t)d.ntypes * d.ntypes);
+        for (size_t q = 0; q < w.matrix.size(); ++q) w.matrix[q] = (float)d.matrix[q];
+        w.p_off = p;
+        w.c_off = c;
+        w.m_off = m;
+        w.b_off = bo;
+        p += w.n;
+        c += w.ncells;
+        m += (int64_t)w.matrix.size();
+        bo += (int64_t)w.bounds.size();
+        next.push_back(std::move(w));
+    }
+    if (p > b->pcap) return berr(b, PLG_E_CAPACITY, "batch particle capacity exceeded");
+    if (c > b->ccap) return berr(b, PLG_E_CAPACITY, "batch cell capacity exceeded");
+    if ((int64_t)next.size() > b->wcap) return berr(b, PLG_E_CAPACITY, "batch world capacity exceeded");
+
+    cudaStream_t st = b->stream;
+    int rc;
+    // Survivors move A -> B (the tables of the old layout are no longer used).
+    if (!survivors.empty()) {
+        BCK(b, cudaMemcpyAsync(b->move_new_d, mnew.data(), sizeof(int) * mnew.size(), cudaMemcpyHostToDevice, st));
+        BCK(b, cudaMemcpyAsync(b->move_old_d, mold.data(), sizeof(int) * mold.size(), cudaMemcpyHostToDevice, st));
+        launch_batch_move<D>(st, (int)n_surv, b->move_new_d, b->move_old_d, (int)survivors.size(),
+                             sbuf<D>(b->apt, b->avel, 0), sbuf<D>(b->bpt, b->bvel, 0));
+        BCK(b, cudaGetLastError());
+    }
+    b->worlds = std::move(next);
+    b->n_total = p;
+    b->c_total = c;
+    if ((rc = upload_tables(b))) return rc;  // synchronises: the move tables above are consumed
+    BCK(b, cudaMemsetAsync(b->counts, 0, sizeof(uint32_t) * (size_t)std::max<int64_t>(c, 1), st));
+    BCK(b, cudaMemsetAsync(b->status_d, 0, sizeof(uint32_t), st));
+    // New worlds: converted from the caller's buffers straight into B.
+    for (int32_t a = 0; a < nadd; ++a) {
+        const plg_world_desc& d = add[a];
+        const WorldRec& w = b->worlds[survivors.size() + (size_t)a];
+        if (ids_out) ids_out[a] = w.id;
+        if (w.n == 0) continue;
+        const double* dpos = mapped_host(d.pos);
+        const double* dvel = mapped_host(d.vel);
+        const int32_t* dtype = mapped_host(d.type);
+        const int64_t rows = (w.n + 1) & ~(int64_t)1;
+        if ((!dpos || (d.vel && !dvel) || !dtype) &&
+            (rc = regrow(b, &b->stage, &b->stage_cap, (int64_t)batch_stage_bytes(rows), "staging")))
+            return rc;
+        double* spos = (double*)b->stage;
+        double* svel = spos + 3 * rows;
+        int32_t* stype = (int32_t*)(svel + 3 * rows);
+        if (!dpos) {
+            BCK(b, cudaMemcpyAsync(spos, d.pos, sizeof(double) * 3 * w.n, cudaMemcpyHostToDevice, st));
+            dpos = spos;
+        }
+        if (d.vel && !dvel) {
+            BCK(b, cudaMemcpyAsync(svel, d.vel, sizeof(double) * 3 * w.n, cudaMemcpyHostToDevice, st));
+            dvel = svel;
+        }
+        if (!dtype) {
+            BCK(b, cudaMemcpyAsync(stype, d.type, sizeof(int32_t) * w.n, cudaMemcpyHostToDevice, st));
+            dtype = stype;
+        }
+        Grid g{};
+        g.nx = w.nx;
+        g.ncells = (int)w.ncells;
+        g.inv_cs = (float)(1.0 / w.s.rmax);
+        g.b_nx = w.bounds[w.nx];
+        g.bounds = b->bounds_d + w.b_off;
+        launch_upload<D>(st, (int)w.n, dpos, dvel, dtype, w.ntypes, sbuf<D>(b->bpt, b->bvel, w.p_off),
+                         b->cell + w.p_off, b->rank + w.p_off, b->counts, g, b->status_d, (uint32_t)w.c_off);
+        BCK(b, cudaGetLastError());
+    }
+    std::swap(b->apt, b->bpt);
+    std::swap(b->avel, b->bvel);
+    // Survivors: cells in the new global numbering and the next sort's counts.
+    if (n_surv > 0) {
+        launch_batch_rebin<D>(st, (int)n_surv, sbuf<D>(b->apt, b->avel, 0), b->worlds_d, b->wp_off_d,
+                              (int)survivors.size(), b->cell, b->rank, b->counts);
+        BCK(b, cudaGetLastError());
+    }
+    BCK(b, cudaMemcpyAsync(b->status_h, b->status_d, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    BCK(b, cudaStreamSynchronize(st));
+    if (*b->status_h) return berr(b, PLG_E_DEVICE, "a conversion kernel flagged invalid input");
+    destroy_batch_graph(b);
+    return PLG_OK;
+}
+
+template <int D>
+void enqueue_batch_step(plg_batch* b, const DebugOut* dbg, int32_t* cell_sorted) {
+    cudaStream_t st = b->stream;
+    const int n = (int)b->n_total;
+    const int nc = (int)std::max<int64_t>(b->c_total, 1);
+    cudaMemsetAsync(b->scan_state, 0, sizeof(unsigned long long) * (size_t)(scan_blocks(nc) + 1), st);
+    launch_scan(st, b->counts, nc, b->cstart, b->scan_state, b->status_d, b->defer);
+    launch_scatter(st, n, b->cell, b->rank, b->cstart, b->perm, b->slot_cell);
+    launch_gather<D>(st, n, b->perm, b->slot_cell, b->cstart, sbuf<D>(b->apt, b->avel, 0),
+                     sbuf<D>(b->bpt, b->bvel, 0), cell_sorted);
+    launch_force_batch<D>(st, b->worlds_d, b->wp_off_d, (int)b->worlds.size(), n, b->smem_matrix,
+                          sbuf<D>(b->bpt, b->bvel, 0), b->cstart, sbuf<D>(b->apt, b->avel, 0), b->cell, b->rank,
+                          b->counts, b->defer, dbg);
+}
+
+int enqueue_step(plg_batch* b) {
+    if (b->n_total == 0) return PLG_OK;
+    if (!b->use_graph) {
+        if (b->dim == 2)
+            enqueue_batch_step<2>(b, nullptr, nullptr);
+        else
+            enqueue_batch_step<3>(b, nullptr, nullptr);
+        BCK(b, cudaGetLastError());
+        return PLG_OK;
+    }
+    if (b->graph_dirty || !b->gexec) {
+        destroy_batch_graph(b);
+        cudaGraph_t g = nullptr;
+        BCK(b, cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+        if (b->dim == 2)
+            enqueue_batch_step<2>(b, nullptr, nullptr);
+        else
+            enqueue_batch_step<3>(b, nullptr, nullptr);
+        cudaError_t e = cudaStreamEndCapture(b->stream, &g);
+        if (e != cudaSuccess) return bcuda(b, "cudaStreamEndCapture", e);
+        e = cudaGraphInstantiate(&b->gexec, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) {
+            b->gexec = nullptr;
+            return bcuda(b, "cudaGraphInstantiate", e);
+        }
+        b->graph_dirty = false;
+    }
+    BCK(b, cudaGraphLaunch(b->gexec, b->stream));
+    return PLG_OK;
+}
+
+int wait_batch(plg_batch* b, double timeout_s) {
+    if (timeout_s <= 0) {
+        BCK(b, cudaStreamSynchronize(b->stream));
+    } else {
+        const auto t0 = std::chrono::steady_clock::now();
+        for (;;) {
+            cudaError_t e = cudaStreamQuery(b->stream);
+            if (e == cudaSuccess) break;
+            if (e != cudaErrorNotReady) return bcuda(b, "cudaStreamQuery", e);
+            const double dt = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+            if (dt > timeout_s) return berr(b, PLG_E_TIMEOUT, "batch sync timed out");
+            std::this_thread::sleep_for(std::chrono::microseconds(50));
+        }
+    }
+    BCK(b, cudaMemcpy(b->status_h, b->status_d, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    if (*b->status_h & kDevSpinLimit) {
+        cudaMemset(b->status_d, 0, sizeof(uint32_t));
+        return berr(b, PLG_E_DEVICE, "a bounded device wait ran out (scan look-back)");
+    }
+    return PLG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int plg_batch_create(int32_t dim, int64_t particle_capacity, int32_t world_capacity, int64_t cell_capacity,
+                     plg_batch** out) {
+    if (!out) return PLG_E_INVALID_ARG;
+    *out = nullptr;
+    if (dim != 2 && dim != 3) return PLG_E_INVALID_ARG;
+    if (particle_capacity < 1 || particle_capacity > kMaxParticles) return PLG_E_INVALID_ARG;
+    if (world_capacity < 1 || world_capacity > kMaxBatchWorlds) return PLG_E_INVALID_ARG;
+    if (cell_capacity < 1 || cell_capacity > kMaxCells) return PLG_E_INVALID_ARG;
+    plg_batch* b = new plg_batch();
+    b->dim = dim;
+    b->pcap = particle_capacity;
+    b->wcap = world_capacity;
+    b->ccap = cell_capacity;
+    if (cudaGetDevice(&b->device) != cudaSuccess) {
+        cudaGetLastError();
+        delete b;
+        return PLG_E_CUDA;
+    }
+    int rc = PLG_OK;
+    auto dm = [&](void** p, size_t bytes) {
+        if (rc) return;
+        if (cudaMalloc(p, bytes) != cudaSuccess) {
+            cudaGetLastError();
+            rc = PLG_E_NO_MEMORY;
+        }
+    };
+    if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess) rc = PLG_E_CUDA;
+    if (!rc && force_kernels_init() != cudaSuccess) rc = PLG_E_CUDA;
+    const size_t pc = (size_t)particle_capacity, cc = (size_t)cell_capacity, wc = (size_t)world_capacity;
+    const size_t vel_sz = dim == 2 ? sizeof(float2) : sizeof(float4);
+    dm((void**)&b->apt, sizeof(float4) * pc);
+    dm((void**)&b->bpt, sizeof(float4) * pc);
+    dm(&b->avel, vel_sz * pc);
+    dm(&b->bvel, vel_sz * pc);
+    dm((void**)&b->cell, sizeof(uint32_t) * pc);
+    dm((void**)&b->rank, sizeof(uint32_t) * pc);
+    dm((void**)&b->perm, sizeof(uint32_t) * pc);
+    dm((void**)&b->slot_cell, sizeof(uint32_t) * pc);
+    dm((void**)&b->counts, sizeof(uint32_t) * cc);
+    dm((void**)&b->cstart, sizeof(uint32_t) * (cc + 1));
+    dm((void**)&b->scan_state, sizeof(unsigned long long) * (size_t)(scan_blocks((int)cc) + 1));
+    dm((void**)&b->defer, sizeof(uint32_t));
+    dm((void**)&b->status_d, 64);
+    dm((void**)&b->worlds_d, sizeof(ForceParams) * wc);
+    dm((void**)&b->wp_off_d, sizeof(int) * (wc + 1));
+    dm((void**)&b->move_new_d, sizeof(int) * (wc + 1));
+    dm((void**)&b->move_old_d, sizeof(int) * wc);
+    if (!rc && cudaMallocHost((void**)&b->status_h, 64) != cudaSuccess) rc = PLG_E_NO_MEMORY;
+    if (!rc && cudaMemset(b->status_d, 0, 64) != cudaSuccess) rc = PLG_E_CUDA;
+    if (!rc && cudaMemset(b->counts, 0, sizeof(uint32_t) * cc) != cudaSuccess) rc = PLG_E_CUDA;
+    if (rc) {
+        cudaGetLastError();
+        free_batch(b);
+        delete b;
+        return rc;
+    }
+    *out = b;
+    return PLG_OK;
+}
+
+int plg_batch_destroy(plg_batch* b) {
+    if (!b) return PLG_E_INVALID_ARG;
+    BatchDeviceGuard g(b->device);
+    cudaStreamSynchronize(b->stream);
+    free_batch(b);
+    delete b;
+    return PLG_OK;
+}
+
+int plg_batch_update(plg_batch* b, int32_t nremove, const int32_t* remove_ids, int32_t nadd,
+                     const plg_world_desc* add, int32_t* ids_out) {
+    if (!b) return PLG_E_INVALID_ARG;
+    if (nremove < 0 || nadd < 0) return berr(b, PLG_E_INVALID_ARG, "negative world count");
+    if ((nremove > 0 && !remove_ids) || (nadd > 0 && !add)) return berr(b, PLG_E_INVALID_ARG, "NULL world list");
+    std::vector<char> gone(b->worlds.size(), 0);
+    for (int32_t r = 0; r < nremove; ++r) {
+        const int k = find_world(b, remove_ids[r]);
+        if (k < 0) return berr(b, PLG_E_INVALID_ARG, "unknown world id " + std::to_string(remove_ids[r]));
+        gone[(size_t)k] = 1;
+    }
+    for (int32_t a = 0; a < nadd; ++a) {
+        const int rc = check_desc(b, add[a]);
+        if (rc) return rc;
+    }
+    std::vector<int> survivors;
+    for (size_t k = 0; k < b->worlds.size(); ++k)
+        if (!gone[k]) survivors.push_back((int)k);
+    BatchDeviceGuard g(b->device);
+    return b->dim == 2 ? relayout<2>(b, survivors, add, nadd, ids_out) : relayout<3>(b, survivors, add, nadd, ids_out);
+}
+
+int plg_batch_step_async(plg_batch* b, int32_t nsteps) {
+    if (!b) return PLG_E_INVALID_ARG;
+    if (nsteps < 0) return berr(b, PLG_E_INVALID_ARG, "negative step count");
+    BatchDeviceGuard g(b->device);
+    for (int32_t k = 0; k < nsteps; ++k) {
+        const int rc = enqueue_step(b);
+        if (rc) return rc;
+    }
+    return PLG_OK;
+}
+
+int plg_batch_sync(plg_batch* b, double timeout_s) {
+    if (!b) return PLG_E_INVALID_ARG;
+    BatchDeviceGuard g(b->device);
+    return wait_batch(b, timeout_s);
+}
+
+int plg_batch_step(plg_batch* b, int32_t nsteps) {
+    const int rc = plg_batch_step_async(b, nsteps);
+    if (rc) return rc;
+    return plg_batch_sync(b, 0.0);
+}
+
+int plg_batch_download(plg_batch* b, int32_t id, double* pos, double* vel, int32_t* type, int32_t* pid) {
+    if (!b) return PLG_E_INVALID_ARG;
+    const int k = find_world(b, id);
+    if (k < 0) return berr(b, PLG_E_INVALID_ARG, "unknown world id " + std::to_string(id));
+    const WorldRec& w = b->worlds[(size_t)k];
+    BatchDeviceGuard g(b->device);
+    cudaStream_t st = b->stream;
+    if (w.n == 0) return PLG_OK;
+    const int64_t rows = (w.n + 1) & ~(int64_t)1;
+    double* mpos = mapped_host(pos);
+    double* mvel = mapped_host(vel);
+    int32_t* mtype = mapped_host(type);
+    int32_t* mid = mapped_host(pid);
+    int rc;
+    if (((pos && !mpos) || (vel && !mvel) || (type && !mtype) || (pid && !mid)) &&
+        (rc = regrow(b, &b->stage, &b->stage_cap, (int64_t)batch_stage_bytes(rows), "staging")))
+        return rc;
+    double* spos = (double*)b->stage;
+    double* svel = spos + 3 * rows;
+    int32_t* stype = (int32_t*)(svel + 3 * rows);
+    int32_t* sid = stype + rows;
+    double* kpos = pos ? (mpos ? mpos : spos) : nullptr;
+    double* kvel = vel ? (mvel ? mvel : svel) : nullptr;
+    int32_t* ktype = type ? (mtype ? mtype : stype) : nullptr;
+    int32_t* kid = pid ? (mid ? mid : sid) : nullptr;
+    if (b->dim == 2)
+        launch_download<2>(st, (int)w.n, sbuf<2>(b->apt, b->avel, w.p_off), kpos, kvel, ktype, kid);
+    else
+        launch_download<3>(st, (int)w.n, sbuf<3>(b->apt, b->avel, w.p_off), kpos, kvel, ktype, kid);
+    BCK(b, cudaGetLastError());
+    const size_t n = (size_t)w.n;
+    if (pos && !mpos) BCK(b, cudaMemcpyAsync(pos, spos, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, st));
+    if (vel && !mvel) BCK(b, cudaMemcpyAsync(vel, svel, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, st));
+    if (type && !mtype) BCK(b, cudaMemcpyAsync(type, stype, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, st));
+    if (pid && !mid) BCK(b, cudaMemcpyAsync(pid, sid, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, st));
+    BCK(b, cudaStreamSynchronize(st));
+    return PLG_OK;
+}
+
+int plg_batch_world_info(plg_batch* b, int32_t id, int64_t* n, int64_t* first_slot, int64_t* first_cell) {
+    if (!b) return PLG_E_INVALID_ARG;
+    const int k = find_world(b, id);
+    if (k < 0) return berr(b, PLG_E_INVALID_ARG, "unknown world id " + std::to_string(id));
+    if (n) *n = b->worlds[(size_t)k].n;
+    if (first_slot) *first_slot = b->worlds[(size_t)k].p_off;
+    if (first_cell) *first_cell = b->worlds[(size_t)k].c_off;
+    return PLG_OK;
+}
+
+int plg_batch_counts(plg_batch* b, int32_t* nworlds, int64_t* nparticles, int64_t* ncells) {
+    if (!b) return PLG_E_INVALID_ARG;
+    if (nworlds) *nworlds = (int32_t)b->worlds.size();
+    if (nparticles) *nparticles = b->n_total;
+    if (ncells) *ncells = b->c_total;
+    return PLG_OK;
+}
+
+int plg_batch_set_use_graph(plg_batch* b, int32_t on) {
+    if (!b) return PLG_E_INVALID_ARG;
+    b->use_graph = on != 0;
+    return PLG_OK;
+}
+
+int plg_batch_get_stream(plg_batch* b, void** stream) {
+    if (!b || !stream) return PLG_E_INVALID_ARG;
+    *stream = (void*)b->stream;
+    return PLG_OK;
+}
+
+const char* plg_batch_last_error(plg_batch* b) { return b ? b->err.c_str() : "null batch"; }
+
+int plg_batch_step_stats(plg_batch* b, int64_t* deferred) {
+    if (!b || !deferred) return PLG_E_INVALID_ARG;
+    BatchDeviceGuard g(b->device);
+    BCK(b, cudaMemcpyAsync(b->status_h + 1, b->defer, sizeof(uint32_t), cudaMemcpyDeviceToHost, b->stream));
+    BCK(b, cudaStreamSynchronize(b->stream));
+    *deferred = b->status_h[1];
+    return PLG_OK;
+}
+
+int plg_batch_debug_step(plg_batch* b, int32_t* cell, int32_t* pairs, uint64_t* hash_sum, uint64_t* hash_xor,
+                         float* acc, int64_t* candidates) {
+    if (!b) return PLG_E_INVALID_ARG;
+    BatchDeviceGuard g(b->device);
+    const size_t cap = (size_t)b->pcap;
+    int rc = PLG_OK;
+    auto dm = [&](void** p, size_t bytes) {
+        if (rc || *p) return;
+        if (cudaMalloc(p, bytes) != cudaSuccess) {
+            cudaGetLastError();
+            *p = nullptr;
+            rc = berr(b, PLG_E_NO_MEMORY, "cudaMalloc (debug buffers)");
+        }
+    };
+    dm((void**)&b->dbg_pairs, sizeof(int32_t) * cap);
+    dm((void**)&b->dbg_hsum, sizeof(unsigned long long) * cap);
+    dm((void**)&b->dbg_hxor, sizeof(unsigned long long) * cap);
+    dm((void**)&b->dbg_cand, sizeof(unsigned long long));
+    dm((void**)&b->dbg_acc, sizeof(float) * 3 * cap);
+    dm((void**)&b->dbg_cell, sizeof(int32_t) * cap);
+    if (rc) return rc;
+    cudaStream_t st = b->stream;
+    BCK(b, cudaMemsetAsync(b->dbg_cand, 0, sizeof(unsigned long long), st));
+    const DebugOut dbg{b->dbg_pairs, b->dbg_hsum, b->dbg_hxor, b->dbg_acc, b->dbg_cand};
+    if (b->n_total > 0) {
+        if (b->dim == 2)
+            enqueue_batch_step<2>(b, &dbg, b->dbg_cell);
+        else
+            enqueue_batch_step<3>(b, &dbg, b->dbg_cell);
+        BCK(b, cudaGetLastError());
+    }
+    const size_t n = (size_t)b->n_total;
+    if (n > 0) {
+        if (cell) BCK(b, cudaMemcpyAsync(cell, b->dbg_cell, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, st));
+        if (pairs) BCK(b, cudaMemcpyAsync(pairs, b->dbg_pairs, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, st));
+        if (hash_sum) BCK(b, cudaMemcpyAsync(hash_sum, b->dbg_hsum, 8 * n, cudaMemcpyDeviceToHost, st));
+        if (hash_xor) BCK(b, cudaMemcpyAsync(hash_xor, b->dbg_hxor, 8 * n, cudaMemcpyDeviceToHost, st));
+        if (acc) BCK(b, cudaMemcpyAsync(acc, b->dbg_acc, sizeof(float) * b->dim * n, cudaMemcpyDeviceToHost, st));
+    }
+    unsigned long long cand = 0;
+    BCK(b, cudaMemcpyAsync(&cand, b->dbg_cand, sizeof(cand), cudaMemcpyDeviceToHost, st));
+    rc = wait_batch(b, 0.0);
+    if (candidates) *candidates = (int64_t)cand;
+    return rc;
+}
+
+}  // extern "C"

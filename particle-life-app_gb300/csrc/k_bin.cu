@@ -63,7 +63,7 @@ __global__ void __launch_bounds__(kThreads) k_upload(int n, const double* __rest
                                                      const int32_t* __restrict__ type, int ntypes,
                                                      StateBuf<D> a, uint32_t* __restrict__ cell,
                                                      uint32_t* __restrict__ rank, uint32_t* counts, Grid g,
-                                                     uint32_t* status, bool vec) {
+                                                     uint32_t* status, bool vec, uint32_t cell_base) {
     __shared__ __align__(16) double sp[3 * kThreads];
     __shared__ __align__(16) double sv[3 * kThreads];
     const int i0 = blockIdx.x * kThreads;
@@ -111,8 +111,42 @@ __global__ void __launch_bounds__(kThreads) k_upload(int n, const double* __rest
             a.pt[i] = make_float4(p[0], p[1], p[2], __int_as_float(ty));
             reinterpret_cast<float4*>(a.vel)[i] = make_float4(v[0], v[1], v[2], __int_as_float(i));
         }
-        c = cell_index<D>(p[0], p[1], p[2], g);
+        c = cell_base + cell_index<D>(p[0], p[1], p[2], g);
         if (bad) atomicOr(status, bad);
+    }
+    const unsigned mask = __ballot_sync(kFull, valid);
+    if (valid) {
+        rank[i] = bin_count(counts, c, mask);
+        cell[i] = c;
+    }
+}
+
+// ---- batched worlds ----
+
+template <int D>
+__global__ void __launch_bounds__(kThreads) k_batch_move(int n, const int* __restrict__ new_off,
+                                                         const int* __restrict__ old_off, int nw, StateBuf<D> a,
+                                                         StateBuf<D> b) {
+    const int s = blockIdx.x * kThreads + threadIdx.x;
+    if (s >= n) return;
+    const int k = world_of(new_off, nw, s);
+    const int src = __ldg(old_off + k) + (s - __ldg(new_off + k));
+    b.pt[s] = a.pt[src];
+    b.vel[s] = a.vel[src];
+}
+
+template <int D>
+__global__ void __launch_bounds__(kThreads) k_batch_rebin(int n, StateBuf<D> a, const ForceParams* __restrict__ worlds,
+                                                          const int* __restrict__ wp_off, int nw,
+                                                          uint32_t* __restrict__ cell, uint32_t* __restrict__ rank,
+                                                          uint32_t* counts) {
+    const int i = blockIdx.x * kThreads + threadIdx.x;
+    const bool valid = i < n;
+    uint32_t c = 0;
+    if (valid) {
+        const ForceParams& P = worlds[world_of(wp_off, nw, i)];
+        const float4 p = a.pt[i];
+        c = P.cell_base + cell_index<D>(p.x, p.y, D == 3 ? p.z : 0.f, P.g);
     }
     const unsigned mask = __ballot_sync(kFull, valid);
     if (valid) {
@@ -352,12 +386,34 @@ inline bool aligned16(const void* p) { return ((uintptr_t)p & 15u) == 0; }
 
 template <int D>
 void launch_upload(cudaStream_t st, int n, const double* pos, const double* vel, const int32_t* type, int ntypes,
-                   StateBuf<D> a, uint32_t* cell, uint32_t* rank, uint32_t* counts, Grid g, uint32_t* status) {
+                   StateBuf<D> a, uint32_t* cell, uint32_t* rank, uint32_t* counts, Grid g, uint32_t* status,
+                   uint32_t cell_base) {
     if (n <= 0) return;
     const bool vec = aligned16(pos) && aligned16(vel);
     k_upload<D><<<blocks_for(n, kThreads), kThreads, 0, st>>>(n, pos, vel, type, ntypes, a, cell, rank, counts, g,
-                                                              status, vec);
+                                                              status, vec, cell_base);
 }
+
+template <int D>
+void launch_batch_move(cudaStream_t st, int n, const int* new_off, const int* old_off, int nw, StateBuf<D> a,
+                       StateBuf<D> b) {
+    if (n <= 0 || nw <= 0) return;
+    k_batch_move<D><<<blocks_for(n, kThreads), kThreads, 0, st>>>(n, new_off, old_off, nw, a, b);
+}
+
+template <int D>
+void launch_batch_rebin(cudaStream_t st, int n, StateBuf<D> a, const ForceParams* worlds, const int* wp_off, int nw,
+                        uint32_t* cell, uint32_t* rank, uint32_t* counts) {
+    if (n <= 0 || nw <= 0) return;
+    k_batch_rebin<D><<<blocks_for(n, kThreads), kThreads, 0, st>>>(n, a, worlds, wp_off, nw, cell, rank, counts);
+}
+
+template void launch_batch_move<2>(cudaStream_t, int, const int*, const int*, int, StateBuf<2>, StateBuf<2>);
+template void launch_batch_move<3>(cudaStream_t, int, const int*, const int*, int, StateBuf<3>, StateBuf<3>);
+template void launch_batch_rebin<2>(cudaStream_t, int, StateBuf<2>, const ForceParams*, const int*, int, uint32_t*,
+                                    uint32_t*, uint32_t*);
+template void launch_batch_rebin<3>(cudaStream_t, int, StateBuf<3>, const ForceParams*, const int*, int, uint32_t*,
+                                    uint32_t*, uint32_t*);
 
 template <int D>
 void launch_rebin(cudaStream_t st, int n, StateBuf<D> a, uint32_t* cell, uint32_t* rank, uint32_t* counts, Grid g) {
@@ -393,9 +449,9 @@ void launch_gather(cudaStream_t st, int n, const uint32_t* perm, const uint32_t*
 }
 
 template void launch_upload<2>(cudaStream_t, int, const double*, const double*, const int32_t*, int, StateBuf<2>,
-                               uint32_t*, uint32_t*, uint32_t*, Grid, uint32_t*);
+                               uint32_t*, uint32_t*, uint32_t*, Grid, uint32_t*, uint32_t);
 template void launch_upload<3>(cudaStream_t, int, const double*, const double*, const int32_t*, int, StateBuf<3>,
-                               uint32_t*, uint32_t*, uint32_t*, Grid, uint32_t*);
+                               uint32_t*, uint32_t*, uint32_t*, Grid, uint32_t*, uint32_t);
 template void launch_rebin<2>(cudaStream_t, int, StateBuf<2>, uint32_t*, uint32_t*, uint32_t*, Grid);
 template void launch_rebin<3>(cudaStream_t, int, StateBuf<3>, uint32_t*, uint32_t*, uint32_t*, Grid);
 template void launch_download<2>(cudaStream_t, int, StateBuf<2>, double*, double*, int32_t*, int32_t*);

@@ -67,7 +67,14 @@ struct ForceArgs {
     uint32_t* counts;
     uint32_t* defer_count;  // targets the tiled kernel deferred this step (statistics)
     DebugOut dbg;
+    // Batched worlds: per-world parameters and first sorted slots
+    // (wp_off[k] = worlds[k].p_off, nworlds + 1 entries).
+    const ForceParams* __restrict__ worlds;
+    const int* __restrict__ wp_off;
+    int nworlds;
+    int n_total;
 };
+
 
 struct Acc {
     float x, y, z;
@@ -187,10 +194,10 @@ __device__ __forceinline__ void fast_pair(const ForceParams& P, float a, float d
 //   candidate     (qox, qoy, qoz): -1 on an axis where the run's own
 //                 coordinates are shifted down (image below the box)
 template <int D, bool DBG>
-__device__ __noinline__ Acc warp_stencil(const ForceArgs<D>& A, const float* Mrow, int s, float px, float py,
-                                         float pz, int slmask, int lane) {
+__device__ __noinline__ Acc warp_stencil(const ForceArgs<D>& A, const ForceParams& P, const uint32_t* cs,
+                                         const float* Mrow, int s, float px, float py, float pz, int slmask,
+                                         int lane) {
     constexpr int R = D == 3 ? 9 : 3;
-    const ForceParams& P = A.p;
     const int nx = P.g.nx;
     const int cx = axis_cell(px, P.g), cy = axis_cell(py, P.g), cz = D == 3 ? axis_cell(pz, P.g) : 0;
     int j0 = 0, len = 0;
@@ -234,8 +241,8 @@ __device__ __noinline__ Acc warp_stencil(const ForceArgs<D>& A, const float* Mro
             }
         }
         if (cb > ca) {
-            j0 = (int)__ldg(A.cstart + base + ca);
-            len = (int)__ldg(A.cstart + base + cb) - j0;
+            j0 = (int)__ldg(cs + base + ca);
+            len = (int)__ldg(cs + base + cb) - j0;
         }
     }
     int inc = len;
@@ -358,8 +365,8 @@ __device__ __forceinline__ float ensure_position(float x, int wrap) {
 // x = v dt + x, ensurePosition; the next state goes to A[s].  Returns the
 // new cell.
 template <int D, bool DBG>
-__device__ __forceinline__ uint32_t integrate(const ForceArgs<D>& A, int s, const float4& me, const Acc& acc) {
-    const ForceParams& P = A.p;
+__device__ __forceinline__ uint32_t integrate(const ForceArgs<D>& A, const ForceParams& P, int s, const float4& me,
+                                              const Acc& acc) {
     typename Layout<D>::Vel v = A.bvel[s];
     const float vx = fmaf(acc.x, P.scale, v.x * P.ff);
     const float vy = fmaf(acc.y, P.scale, v.y * P.ff);
@@ -386,7 +393,7 @@ __device__ __forceinline__ uint32_t integrate(const ForceArgs<D>& A, int s, cons
         }
         if (A.dbg.candidates) atomicAdd(A.dbg.candidates, acc.cand);
     }
-    return cell_index<D>(nxp, nyp, nzp, A.p.g);
+    return P.cell_base + cell_index<D>(nxp, nyp, nzp, P.g);
 }
 
 template <int D>
@@ -415,7 +422,7 @@ __global__ void __launch_bounds__(kThreads) k_force_general(const __grid_constan
         const float4 me = A.bpt[s];
         Acc acc = {0.f, 0.f, 0.f, 0, 0ull, 0ull, 0ull};
         general_scan<D, DBG>(A, M + Layout<D>::type(me) * P.ntypes, s, me.x, me.y, D == 3 ? me.z : 0.f, acc);
-        newcell = integrate<D, DBG>(A, s, me, acc);
+        newcell = integrate<D, DBG>(A, A.p, s, me, acc);
     }
     const unsigned mask = __ballot_sync(kFull, valid);
     if (valid) {
@@ -508,15 +515,15 @@ __device__ __forceinline__ int block_scan_inplace(int* v, int n, int* wsum) {
 // are shifted down by 1 here (exact: their coordinates are >= 0.5); images
 // above it are flagged for a target shift instead.
 template <int D>
-__device__ __forceinline__ void stage_segment(const ForceArgs<D>& A, TileSmem<D>& sm, int srow, int cxa, int cxb) {
+__device__ __forceinline__ void stage_segment(const ForceArgs<D>& A, const ForceParams& P,
+                                              const uint32_t* __restrict__ cs, TileSmem<D>& sm, int srow, int cxa,
+                                              int cxb) {
     constexpr int R = TileRows<D>::R;
-    const ForceParams& P = A.p;
     const int nx = P.g.nx;
     const int tid = threadIdx.x;
     const int cy = D == 3 ? srow % nx : srow, cz = D == 3 ? srow / nx : 0;
     const int ncols = cxb - cxa + 1;
     const int ncell = R * (ncols + 2);
-    const uint32_t* __restrict__ cs = A.cstart;
     if (ncell > TileCfg<D>::kCells) {
         if (tid == 0) sm.staged = 0;
         __syncthreads();
@@ -606,10 +613,9 @@ __device__ __forceinline__ float rsqrt_approx(float x) {
 // this partial sum.  SHIFT: the segment touches the box's upper boundary,
 // so some candidates carry target-shift flags.
 template <int D, bool DBG, bool SHIFT>
-__device__ __forceinline__ bool tile_range(const ForceArgs<D>& A, const TileSmem<D>& sm,
+__device__ __forceinline__ bool tile_range(const ForceArgs<D>& A, const ForceParams& P, const TileSmem<D>& sm,
                                            const float* __restrict__ Mrow, int ncell, int ja, int jb, float px,
                                            float py, float pz, Acc& acc) {
-    const ForceParams& P = A.p;
     const float px1 = px - 1.f, py1 = py - 1.f, pz1 = pz - 1.f;
     bool rare = false;
     // Loop constants in registers (read once, not per candidate).
@@ -666,11 +672,11 @@ __device__ __forceinline__ float warp_sum(float v) {
 // global-memory stencil (with the FP64 decisions), their partial sums are
 // combined by warp_sum, and lane 0 runs the epilogue and the counting step.
 template <int D, bool DBG>
-__device__ __noinline__ void fixup_target(const ForceArgs<D>& A, const float* M, int s, int lane) {
-    const ForceParams& P = A.p;
+__device__ __noinline__ void fixup_target(const ForceArgs<D>& A, const ForceParams& P, const uint32_t* cs,
+                                          const float* M, int s, int lane) {
     const float4 me = A.bpt[s];
     const float px = me.x, py = me.y, pz = D == 3 ? me.z : 0.f;
-    Acc acc = warp_stencil<D, DBG>(A, M + Layout<D>::type(me) * P.ntypes, s, px, py, pz,
+    Acc acc = warp_stencil<D, DBG>(A, P, cs, M + Layout<D>::type(me) * P.ntypes, s, px, py, pz,
                                    sliver_mask<D>(P, px, py, pz), lane);
     acc.x = warp_sum(acc.x);
     acc.y = warp_sum(acc.y);
@@ -685,36 +691,49 @@ __device__ __noinline__ void fixup_target(const ForceArgs<D>& A, const float* M,
         }
     }
     if (lane == 0) {
-        const uint32_t newcell = integrate<D, DBG>(A, s, me, acc);
+        const uint32_t newcell = integrate<D, DBG>(A, P, s, me, acc);
         A.rank[s] = atomicAdd(A.counts + newcell, 1u);
         A.cell[s] = newcell;
     }
 }
 
+// Segment key of a target: its grid row, and in a batch its world in the
+// bits above kRowBits (worlds < 2^10, rows < 2^21).
+constexpr int kRowBits = 21;
+constexpr int kRowMask = (1 << kRowBits) - 1;
+
 // Main force kernel (nx >= 3): one thread per target; a block takes 256 (3D: 128)
-// consecutive targets and, per segment (targets of one grid row), stages the
-// segment's stencil so that each target reads one contiguous run.  FP32 only
-// and call-free: a target whose run meets a candidate that needs the FP64
-// decision, or whose segment did not fit in shared memory, is deferred to
-// the block's closing pass (fixup_target), which recomputes it completely.
-template <int D, bool DBG, bool SMEM_M>
-__global__ void __launch_bounds__(TileCfg<D>::kTargets, TileCfg<D>::kMinBlocks) k_force_tile(const __grid_constant__ ForceArgs<D> A) {
+// consecutive targets and, per segment (targets of one grid row of one
+// world), stages the segment's stencil so that each target reads one
+// contiguous run.  FP32 only and call-free: a target whose run meets a
+// candidate that needs the FP64 decision, or whose segment did not fit in
+// shared memory, is deferred to the block's closing pass (fixup_target),
+// which recomputes it completely.
+// BATCH: the sorted order holds many worlds one after another (their cells
+// are disjoint ranges of one global cell index); each target finds its
+// world's parameters in A.worlds, and segments never mix worlds, so every
+// target computes exactly what a single-world launch would.
+template <int D, bool DBG, bool SMEM_M, bool BATCH>
+__global__ void __launch_bounds__(TileCfg<D>::kTargets, TileCfg<D>::kMinBlocks)
+    k_force_tile(const __grid_constant__ ForceArgs<D> A) {
     constexpr int kT = TileCfg<D>::kTargets;
     constexpr int R = TileRows<D>::R;
     extern __shared__ __align__(16) unsigned char smraw[];
     TileSmem<D>& sm = *reinterpret_cast<TileSmem<D>*>(smraw);
-    const ForceParams& P = A.p;
     const int tid = threadIdx.x;
-    const int nx = P.g.nx;
-    if (SMEM_M) {
+    const int ntot = BATCH ? A.n_total : A.p.n;
+    const int s0 = blockIdx.x * kT;
+    const int nvalid = min(kT, ntot - s0);
+    const bool valid = tid < nvalid;
+    const int s = s0 + tid;
+    int wk = 0;
+    if (BATCH && valid) wk = world_of(A.wp_off, A.nworlds, s);
+    const ForceParams& P = BATCH ? A.worlds[wk] : A.p;
+    if (SMEM_M && !BATCH) {
         const int nn = P.ntypes * P.ntypes;
         for (int k = tid; k < nn; k += kT) sm.mat[k] = P.matrix[k];
     }
     const float* M = SMEM_M ? sm.mat : P.matrix;
-    const int s0 = blockIdx.x * kT;
-    const int nvalid = min(kT, P.n - s0);
-    const bool valid = tid < nvalid;
-    const int s = s0 + tid;
     float4 me = make_float4(0.f, 0.f, 0.f, 0.f);
     int cx = 0, row = INT_MAX;
     if (valid) {
@@ -722,7 +741,8 @@ __global__ void __launch_bounds__(TileCfg<D>::kTargets, TileCfg<D>::kMinBlocks) 
         cx = axis_cell(me.x, P.g);
         const int cy = axis_cell(me.y, P.g);
         const int cz = D == 3 ? axis_cell(me.z, P.g) : 0;
-        row = cy + cz * nx;
+        row = cy + cz * P.g.nx;
+        if (BATCH) row |= wk << kRowBits;
     }
     sm.rowid[tid] = row;
     sm.colid[tid] = cx;
@@ -750,11 +770,20 @@ __global__ void __launch_bounds__(TileCfg<D>::kTargets, TileCfg<D>::kMinBlocks) 
     bool defer = false;
     for (int g = 0; g < nseg; ++g) {
         const int ta = sm.seg[g], tb = sm.seg[g + 1];
-        const int srow = sm.rowid[ta];
+        const int key = sm.rowid[ta];
+        const int srow = BATCH ? key & kRowMask : key;
         const int cxa = sm.colid[ta], cxb = sm.colid[tb - 1];
-        stage_segment<D>(A, sm, srow, cxa, cxb);
+        const ForceParams& SP = BATCH ? A.worlds[key >> kRowBits] : A.p;  // the segment's world
+        if (SMEM_M && BATCH) {
+            // The previous segment's readers passed the barrier that ends its
+            // iteration; stage_segment's first barrier publishes the matrix.
+            const int nn = SP.ntypes * SP.ntypes;
+            for (int k = tid; k < nn; k += kT) sm.mat[k] = SP.matrix[k];
+        }
+        stage_segment<D>(A, SP, A.cstart + SP.cell_base, sm, srow, cxa, cxb);
         if (tid >= ta && tid < tb) {
             if (sm.staged) {
+                const int nx = P.g.nx;
                 const int ncell = R * (cxb - cxa + 3);
                 const int k = cx - cxa + 1;  // stencil column of the target
                 const int j0 = sm.coff[(k - 1) * R], j1 = sm.coff[(k + 2) * R];
@@ -764,11 +793,11 @@ __global__ void __launch_bounds__(TileCfg<D>::kTargets, TileCfg<D>::kMinBlocks) 
                 const bool shift = P.wrap && (cxb == nx - 1 || cy == nx - 1 || (D == 3 && cz == nx - 1));
                 // The target itself splits its run: [j0, self_j) and (self_j, j1).
                 if (shift) {
-                    defer = tile_range<D, DBG, true>(A, sm, Mrow, ncell, j0, self_j, px, py, pz, acc);
-                    defer |= tile_range<D, DBG, true>(A, sm, Mrow, ncell, self_j + 1, j1, px, py, pz, acc);
+                    defer = tile_range<D, DBG, true>(A, P, sm, Mrow, ncell, j0, self_j, px, py, pz, acc);
+                    defer |= tile_range<D, DBG, true>(A, P, sm, Mrow, ncell, self_j + 1, j1, px, py, pz, acc);
                 } else {
-                    defer = tile_range<D, DBG, false>(A, sm, Mrow, ncell, j0, self_j, px, py, pz, acc);
-                    defer |= tile_range<D, DBG, false>(A, sm, Mrow, ncell, self_j + 1, j1, px, py, pz, acc);
+                    defer = tile_range<D, DBG, false>(A, P, sm, Mrow, ncell, j0, self_j, px, py, pz, acc);
+                    defer |= tile_range<D, DBG, false>(A, P, sm, Mrow, ncell, self_j + 1, j1, px, py, pz, acc);
                 }
             } else {
                 defer = true;
@@ -778,7 +807,7 @@ __global__ void __launch_bounds__(TileCfg<D>::kTargets, TileCfg<D>::kMinBlocks) 
     }
     const bool done = valid && !defer;
     uint32_t newcell = 0;
-    if (done) newcell = integrate<D, DBG>(A, s, me, acc);
+    if (done) newcell = integrate<D, DBG>(A, P, s, me, acc);
     const unsigned mask = __ballot_sync(kFull, done);
     if (done) {
         A.rank[s] = bin_count(A.counts, newcell, mask);
@@ -801,7 +830,17 @@ __global__ void __launch_bounds__(TileCfg<D>::kTargets, TileCfg<D>::kMinBlocks) 
     if (valid && defer) sm.rowid[dbefore + __popc(dm & ((1u << lane) - 1u))] = s;
     if (tid == 0) atomicAdd(A.defer_count, (uint32_t)nd);
     __syncthreads();
-    for (int d = warp; d < nd; d += kT / 32) fixup_target<D, DBG>(A, M, sm.rowid[d], lane);
+    for (int d = warp; d < nd; d += kT / 32) {
+        const int t = sm.rowid[d];
+        if (BATCH) {
+            // The shared matrix belongs to the last segment's world: use the
+            // target's world's matrix in global memory.
+            const ForceParams& TP = A.worlds[world_of(A.wp_off, A.nworlds, t)];
+            fixup_target<D, DBG>(A, TP, A.cstart + TP.cell_base, TP.matrix, t, lane);
+        } else {
+            fixup_target<D, DBG>(A, A.p, A.cstart, M, t, lane);
+        }
+    }
 }
 
 template <int D, bool DBG>
@@ -820,9 +859,9 @@ void launch_variant(cudaStream_t st, const ForceArgs<D>& A, bool general) {
         const int grid = (n + kT - 1) / kT;
         const size_t sb = sizeof(TileSmem<D>);
         if (smem)
-            k_force_tile<D, DBG, true><<<grid, kT, sb, st>>>(A);
+            k_force_tile<D, DBG, true, false><<<grid, kT, sb, st>>>(A);
         else
-            k_force_tile<D, DBG, false><<<grid, kT, sb, st>>>(A);
+            k_force_tile<D, DBG, false, false><<<grid, kT, sb, st>>>(A);
     }
 }
 
@@ -841,6 +880,10 @@ ForceArgs<D> make_args(const ForceParams& p, StateBuf<D> b, const uint32_t* csta
     A.counts = counts;
     A.defer_count = defer;
     A.dbg = dbg ? *dbg : DebugOut{nullptr, nullptr, nullptr, nullptr, nullptr};
+    A.worlds = nullptr;
+    A.wp_off = nullptr;
+    A.nworlds = 1;
+    A.n_total = p.n;
     return A;
 }
 
@@ -858,22 +901,60 @@ void launch_force(cudaStream_t st, const ForceParams& p, bool general, StateBuf<
         launch_variant<D, false>(st, A, general);
 }
 
+template <int D>
+void launch_force_batch(cudaStream_t st, const ForceParams* worlds, const int* wp_off, int nworlds, int n_total,
+                        bool smem_matrix, StateBuf<D> b, const uint32_t* cstart, StateBuf<D> a, uint32_t* cell,
+                        uint32_t* rank, uint32_t* counts, uint32_t* defer, const DebugOut* dbg) {
+    if (n_total <= 0 || nworlds <= 0) return;
+    ForceParams none{};
+    ForceArgs<D> A = make_args<D>(none, b, cstart, a, cell, rank, counts, defer, dbg);
+    A.worlds = worlds;
+    A.wp_off = wp_off;
+    A.nworlds = nworlds;
+    A.n_total = n_total;
+    constexpr int kT = TileCfg<D>::kTargets;
+    const int grid = (n_total + kT - 1) / kT;
+    const size_t sb = sizeof(TileSmem<D>);
+    if (dbg) {
+        if (smem_matrix)
+            k_force_tile<D, true, true, true><<<grid, kT, sb, st>>>(A);
+        else
+            k_force_tile<D, true, false, true><<<grid, kT, sb, st>>>(A);
+    } else {
+        if (smem_matrix)
+            k_force_tile<D, false, true, true><<<grid, kT, sb, st>>>(A);
+        else
+            k_force_tile<D, false, false, true><<<grid, kT, sb, st>>>(A);
+    }
+}
+
+template void launch_force_batch<2>(cudaStream_t, const ForceParams*, const int*, int, int, bool, StateBuf<2>,
+                                    const uint32_t*, StateBuf<2>, uint32_t*, uint32_t*, uint32_t*, uint32_t*,
+                                    const DebugOut*);
+template void launch_force_batch<3>(cudaStream_t, const ForceParams*, const int*, int, int, bool, StateBuf<3>,
+                                    const uint32_t*, StateBuf<3>, uint32_t*, uint32_t*, uint32_t*, uint32_t*,
+                                    const DebugOut*);
+
 template void launch_force<2>(cudaStream_t, const ForceParams&, bool, StateBuf<2>, const uint32_t*, StateBuf<2>,
                               uint32_t*, uint32_t*, uint32_t*, uint32_t*, const DebugOut*);
 template void launch_force<3>(cudaStream_t, const ForceParams&, bool, StateBuf<3>, const uint32_t*, StateBuf<3>,
                               uint32_t*, uint32_t*, uint32_t*, uint32_t*, const DebugOut*);
 
+template <int D, bool DBG, bool SMEM_M, bool BATCH>
+cudaError_t allow_one() {
+    return cudaFuncSetAttribute(k_force_tile<D, DBG, SMEM_M, BATCH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)sizeof(TileSmem<D>));
+}
+
 template <int D>
 cudaError_t allow_tile_smem() {
-    const int sb = (int)sizeof(TileSmem<D>);
-    cudaError_t e = cudaFuncSetAttribute(k_force_tile<D, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sb);
-    if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_force_tile<D, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, sb);
-    if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_force_tile<D, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sb);
-    if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_force_tile<D, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, sb);
-    return e;
+    const cudaError_t es[] = {allow_one<D, false, true, false>(), allow_one<D, false, false, false>(),
+                              allow_one<D, true, true, false>(),  allow_one<D, true, false, false>(),
+                              allow_one<D, false, true, true>(),  allow_one<D, false, false, true>(),
+                              allow_one<D, true, true, true>(),   allow_one<D, true, false, true>()};
+    for (cudaError_t e : es)
+        if (e != cudaSuccess) return e;
+    return cudaSuccess;
 }
 
 cudaError_t force_kernels_init() {

@@ -102,6 +102,20 @@ __host__ __device__ __forceinline__ uint64_t mix64(uint64_t id) {
     return z ^ (z >> 31);
 }
 
+// World of sorted slot s in a batch: the last k with off[k] <= s
+// (off: first slot of each world, ascending).
+__device__ __forceinline__ int world_of(const int* __restrict__ off, int nworlds, int s) {
+    int lo = 0, hi = nworlds;
+    while (hi - lo > 1) {
+        const int m = (lo + hi) >> 1;
+        if (__ldg(off + m) <= s)
+            lo = m;
+        else
+            hi = m;
+    }
+    return lo;
+}
+
 // Parameters of the force / integration kernel, passed by value.
 struct ForceParams {
     Grid g;
@@ -120,6 +134,8 @@ struct ForceParams {
     float scale;            // (float) (rmax * force * dt)
     float dt;
     double rmax, rmax2, beta_d;
+    uint32_t cell_base;     // global index of this world's cell 0 (0 for a single world)
+    int p_off;              // first sorted slot of this world (0 for a single world)
 };
 
 // Per-particle debug outputs of the instrumented force kernel.
@@ -139,10 +155,24 @@ struct StateBuf {
 
 // ---- launchers (defined in the .cu files, called by the host library) ----
 
+// cell_base: added to every cell index (a world's first cell in a batch).
 template <int D>
 void launch_upload(cudaStream_t st, int n, const double* pos, const double* vel, const int32_t* type,
                    int ntypes, StateBuf<D> a, uint32_t* cell, uint32_t* rank, uint32_t* counts, Grid g,
-                   uint32_t* status);
+                   uint32_t* status, uint32_t cell_base = 0);
+
+// Batched worlds: copies surviving worlds to their new places,
+// b[s] = a[old_off[k] + s - new_off[k]] for new_off[k] <= s < new_off[k + 1]
+// (k < nw; new_off has nw + 1 entries).
+template <int D>
+void launch_batch_move(cudaStream_t st, int n, const int* new_off, const int* old_off, int nw, StateBuf<D> a,
+                       StateBuf<D> b);
+
+// Batched worlds: cell and count of every particle in slots [0, n) with its
+// world's grid (worlds[k].cell_base + cell), for the next sort.
+template <int D>
+void launch_batch_rebin(cudaStream_t st, int n, StateBuf<D> a, const ForceParams* worlds, const int* wp_off, int nw,
+                        uint32_t* cell, uint32_t* rank, uint32_t* counts);
 
 template <int D>
 void launch_rebin(cudaStream_t st, int n, StateBuf<D> a, uint32_t* cell, uint32_t* rank, uint32_t* counts,
@@ -171,6 +201,15 @@ template <int D>
 void launch_force(cudaStream_t st, const ForceParams& p, bool general, StateBuf<D> b, const uint32_t* cstart,
                   StateBuf<D> a, uint32_t* cell, uint32_t* rank, uint32_t* counts, uint32_t* defer,
                   const DebugOut* dbg);
+
+// Batched worlds: `worlds` (device, nworlds entries) holds each world's
+// parameters with its cell_base and p_off; `wp_off` (device, nworlds + 1)
+// the first sorted slot of each world and the total.  Every world has
+// nx >= 3.  smem_matrix: every world has at most 16 types.
+template <int D>
+void launch_force_batch(cudaStream_t st, const ForceParams* worlds, const int* wp_off, int nworlds, int n_total,
+                        bool smem_matrix, StateBuf<D> b, const uint32_t* cstart, StateBuf<D> a, uint32_t* cell,
+                        uint32_t* rank, uint32_t* counts, uint32_t* defer, const DebugOut* dbg);
 
 // Opts the tiled force kernel in to its dynamic shared memory (> 48 KB) on
 // the current device; called once per context.

@@ -17,19 +17,68 @@
 #include <thread>
 #include <vector>
 
+#include "plg_host.h"
 #include "plg_internal.cuh"
 #include "plgpu.h"
 
 using namespace plg;
 
+namespace plg {
+
+int grid_n(double rmax) { return (int)std::floor(1 / rmax); }
+
+// (int)((double)x/cs) >= k  <=>  (double)x/cs >= k.
+void build_bounds(double cs, int nx, float* b) {
+    b[0] = 0.f;
+    for (int k = 1; k <= nx; ++k) {
+        float f = (float)(k * cs);
+        while (!((double)f / cs >= (double)k)) f = std::nextafter(f, INFINITY);
+        for (;;) {
+            const float g = std::nextafter(f, -INFINITY);
+            if (g < 0.f || !((double)g / cs >= (double)k)) break;
+            f = g;
+        }
+        b[k] = f;
+    }
+}
+
+void fill_force_params(const plg_settings& s, int nx, int64_t ncells, int ntypes, float b_nx, ForceParams& p) {
+    p.g.nx = nx;
+    p.g.ncells = (int)ncells;
+    p.g.inv_cs = (float)(1.0 / s.rmax);
+    p.g.b_nx = b_nx;
+    p.wrap = s.wrap ? 1 : 0;
+    p.ntypes = ntypes;
+    p.slmask_ok = nx >= 4 ? 1 : 0;
+    const double r2 = s.rmax * s.rmax;
+    const double lo_d = r2 * (1.0 - kBandRel), hi_d = r2 * (1.0 + kBandRel);
+    float lo = (float)lo_d, hi = (float)hi_d;
+    if ((double)lo > lo_d) lo = std::nextafter(lo, 0.f);
+    if ((double)hi < hi_d) hi = std::nextafter(hi, INFINITY);
+    p.lo = lo;
+    p.hi = hi;
+    p.tiny = std::ldexp(1.0f, -100);
+    p.inv_rmax = (float)(1.0 / s.rmax);
+    p.beta = (float)s.beta;
+    p.inv_beta = (float)(1.0 / s.beta);
+    p.one_plus_beta = (float)(1.0 + s.beta);
+    p.inv_one_minus_beta = (float)(1.0 / (1.0 - s.beta));
+    p.m2_inv_rmax = (float)(-2.0 / s.rmax);
+    p.beta_rmax = (float)(s.beta * s.rmax);
+    p.k1 = (float)(1.0 / (s.beta * s.rmax));
+    p.ff = (float)std::pow(s.friction, 60 * s.dt);
+    p.scale = (float)(s.rmax * s.force * s.dt);
+    p.dt = (float)s.dt;
+    p.rmax = s.rmax;
+    p.rmax2 = r2;
+    p.beta_d = s.beta;
+}
+
+}  // namespace plg
+
 namespace {
 
-constexpr int kRing = 4;                        // steps in flight per plg_step call
-constexpr int64_t kMaxParticles = INT_MAX / 2;  // 32-bit indices on the device
-constexpr int64_t kMaxCells = (int64_t)1 << 30;
-constexpr int kMaxAxisCells = 1 << 20;
-constexpr int kMaxTypes = 1024;
-constexpr double kBandRel = 1.0 / (1 << 19);  // FP32 decision band: 2^-19 relative
+constexpr int kRing = 4;  // steps in flight per plg_step call
 
 const char* kKernelNames[PLG_K_COUNT] = {"scan", "scatter", "gather", "force"};
 
@@ -179,24 +228,6 @@ int grow(plg_ctx* c, T** p, int64_t* cap, int64_t need, const char* what) {
     return PLG_OK;
 }
 
-// bounds[k] = smallest float x >= 0 with (double)x / cs >= k (k = 1..nx);
-// bounds[0] = 0.  (int)((double)x/cs) >= k  <=>  (double)x/cs >= k.
-void build_bounds(double cs, int nx, float* b) {
-    b[0] = 0.f;
-    for (int k = 1; k <= nx; ++k) {
-        float f = (float)(k * cs);
-        while (!((double)f / cs >= (double)k)) f = std::nextafter(f, INFINITY);
-        for (;;) {
-            const float g = std::nextafter(f, -INFINITY);
-            if (g < 0.f || !((double)g / cs >= (double)k)) break;
-            f = g;
-        }
-        b[k] = f;
-    }
-}
-
-int grid_n(double rmax) { return (int)std::floor(1 / rmax); }
-
 void destroy_graph(plg_ctx* c) {
     if (c->gexec) cudaGraphExecDestroy(c->gexec);
     c->gexec = nullptr;
@@ -213,40 +244,13 @@ StateBuf<D> buf_b(plg_ctx* c) {
 }
 
 void compute_force_params(plg_ctx* c) {
-    const plg_settings& s = c->s;
     ForceParams& p = c->fp;
-    p.g.nx = c->nx;
-    p.g.ncells = c->ncells;
-    p.g.inv_cs = (float)(1.0 / s.rmax);
-    p.g.b_nx = c->bounds_h[c->nx];
+    fill_force_params(c->s, c->nx, c->ncells, c->ntypes, c->bounds_h[c->nx], p);
     p.g.bounds = c->bounds;
     p.n = (int)c->n;
-    p.wrap = s.wrap ? 1 : 0;
-    p.ntypes = c->ntypes;
-    p.slmask_ok = c->nx >= 4 ? 1 : 0;
     p.matrix = c->matrix;
-    const double r2 = s.rmax * s.rmax;
-    const double lo_d = r2 * (1.0 - kBandRel), hi_d = r2 * (1.0 + kBandRel);
-    float lo = (float)lo_d, hi = (float)hi_d;
-    if ((double)lo > lo_d) lo = std::nextafter(lo, 0.f);
-    if ((double)hi < hi_d) hi = std::nextafter(hi, INFINITY);
-    p.lo = lo;
-    p.hi = hi;
-    p.tiny = std::ldexp(1.0f, -100);
-    p.inv_rmax = (float)(1.0 / s.rmax);
-    p.beta = (float)s.beta;
-    p.inv_beta = (float)(1.0 / s.beta);
-    p.one_plus_beta = (float)(1.0 + s.beta);
-    p.inv_one_minus_beta = (float)(1.0 / (1.0 - s.beta));
-    p.m2_inv_rmax = (float)(-2.0 / s.rmax);
-    p.beta_rmax = (float)(s.beta * s.rmax);
-    p.k1 = (float)(1.0 / (s.beta * s.rmax));
-    p.ff = (float)std::pow(s.friction, 60 * s.dt);
-    p.scale = (float)(s.rmax * s.force * s.dt);
-    p.dt = (float)s.dt;
-    p.rmax = s.rmax;
-    p.rmax2 = r2;
-    p.beta_d = s.beta;
+    p.cell_base = 0;
+    p.p_off = 0;
     c->general = c->nx < 3;
 }
 

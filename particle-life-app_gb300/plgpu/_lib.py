@@ -43,6 +43,18 @@ class plg_settings(C.Structure):
     ]
 
 
+class plg_world_desc(C.Structure):
+    _fields_ = [
+        ("settings", plg_settings),
+        ("ntypes", C.c_int32),
+        ("matrix", C.POINTER(C.c_double)),
+        ("n", C.c_int64),
+        ("pos", C.POINTER(C.c_double)),
+        ("vel", C.POINTER(C.c_double)),
+        ("type", C.POINTER(C.c_int32)),
+    ]
+
+
 class PlgError(RuntimeError):
     """A plg_* call returned a non-zero status."""
 
@@ -86,6 +98,20 @@ SIGNATURES = {
     "plg_probe_fp32_peak": (C.c_int, [_DP]),
     "plg_step_stats": (C.c_int, [_P, _I64P]),
     "plg_sort_cells_noalloc": (C.c_int, [C.c_int32, C.c_double, C.c_int64, _P, _P, _P, _P, _P]),
+    "plg_batch_create": (C.c_int, [C.c_int32, C.c_int64, C.c_int32, C.c_int64, C.POINTER(_P)]),
+    "plg_batch_destroy": (C.c_int, [_P]),
+    "plg_batch_update": (C.c_int, [_P, C.c_int32, _I32P, C.c_int32, C.POINTER(plg_world_desc), _I32P]),
+    "plg_batch_step": (C.c_int, [_P, C.c_int32]),
+    "plg_batch_step_async": (C.c_int, [_P, C.c_int32]),
+    "plg_batch_sync": (C.c_int, [_P, C.c_double]),
+    "plg_batch_download": (C.c_int, [_P, C.c_int32, _DP, _DP, _I32P, _I32P]),
+    "plg_batch_world_info": (C.c_int, [_P, C.c_int32, _I64P, _I64P, _I64P]),
+    "plg_batch_counts": (C.c_int, [_P, _I32P, _I64P, _I64P]),
+    "plg_batch_set_use_graph": (C.c_int, [_P, C.c_int32]),
+    "plg_batch_get_stream": (C.c_int, [_P, C.POINTER(_P)]),
+    "plg_batch_last_error": (C.c_char_p, [_P]),
+    "plg_batch_step_stats": (C.c_int, [_P, _I64P]),
+    "plg_batch_debug_step": (C.c_int, [_P, _I32P, _I32P, _U64P, _U64P, _FP, _I64P]),
 }
 
 _lib = None

@@ -1,0 +1,139 @@
+"""Batched worlds (plg_batch_*): every world of a batch against the oracle
+run on that world alone, and the same world's trajectory alone and in a
+mix, across membership changes, bit for bit."""
+import numpy as np
+import pytest
+
+from worlds import WorldSpec, blob_world, compare_with_oracle, uniform_world
+
+pytestmark = pytest.mark.gpu
+
+
+def desc(spec: WorldSpec):
+    from plgpu.batch import WorldDesc
+
+    return WorldDesc(pos=spec.pos, types=spec.types, matrix=spec.matrix, rmax=spec.rmax, friction=spec.friction,
+                     force=spec.force, dt=spec.dt, beta=spec.beta, wrap=spec.wrap, vel=spec.vel)
+
+
+def make_batch(dim, specs, extra_cells=0):
+    from plgpu.batch import GpuBatch
+
+    ncap = sum(s.n for s in specs) + 1
+    ccap = sum(int(np.floor(1 / s.rmax)) ** dim for s in specs) + extra_cells + 1
+    b = GpuBatch(dim, ncap * 2, 64, ccap * 2)
+    ids = b.update(add=[desc(s) for s in specs])
+    return b, ids
+
+
+def mixed_2d_specs():
+    return [
+        uniform_world(30_000, 6, 0.02, seed=41, vel_scale=0.01),
+        uniform_world(4_000, 3, 0.05, seed=42, vel_scale=0.02, dt=0.01),
+        uniform_world(20_000, 12, 0.0091, seed=43, wrap=False),
+        blob_world(15_000, 5, 0.015, nblobs=8, sigma=0.01, seed=44, dim=2),
+        uniform_world(1_000, 4, 0.3, seed=45),          # nx = 3
+        uniform_world(12_000, 16, 0.0137, seed=46, vel_scale=0.01, dt=0.005),
+    ]
+
+
+def test_batch_2d_every_world_matches_the_oracle(gpu):
+    specs = mixed_2d_specs()
+    b, ids = make_batch(2, specs)
+    dbg = b.debug_step()
+    for spec, wid in zip(specs, ids):
+        g = b.world_debug(dbg, wid)
+        compare_with_oracle(spec, g, b.download(wid))
+    b.close()
+
+
+def test_batch_3d_every_world_matches_the_oracle(gpu):
+    specs = [
+        uniform_world(40_000, 8, 0.04, seed=51, dim=3, vel_scale=0.01, dt=0.01),
+        blob_world(30_000, 16, 0.02, nblobs=6, sigma=0.02, seed=52, dim=3),
+        uniform_world(2_000, 3, 0.26, seed=53, dim=3),
+    ]
+    b, ids = make_batch(3, specs)
+    dbg = b.debug_step()
+    for spec, wid in zip(specs, ids):
+        compare_with_oracle(spec, b.world_debug(dbg, wid), b.download(wid))
+    b.close()
+
+
+def trajectory(b, wid, steps):
+    b.step(steps)
+    return b.download(wid)
+
+
+def test_world_alone_and_in_a_mix_is_bit_identical(gpu):
+    specs = mixed_2d_specs()
+    target = specs[0]
+    alone, (aid,) = make_batch(2, [target])
+    ref = trajectory(alone, aid, 6)
+    alone.close()
+    mix, ids = make_batch(2, specs[3:] + [target] + specs[1:3])
+    got = trajectory(mix, ids[3], 6)
+    mix.close()
+    for a, c in zip(ref, got):
+        assert np.array_equal(a, c)
+
+
+def test_membership_changes_keep_trajectories(gpu):
+    """Removing and adding other worlds between steps does not change a world."""
+    specs = mixed_2d_specs()
+    ref_b, ref_ids = make_batch(2, specs[:2])
+    ref_b.step(3)
+    ref_b.step(4)
+    ref = [ref_b.download(w) for w in ref_ids]
+    ref_b.close()
+
+    b, ids = make_batch(2, specs[:4], extra_cells=10 ** 5)
+    b.step(3)
+    b.update(remove=[ids[2]], add=[desc(specs[5])])
+    b.update(remove=[ids[3]])
+    b.step(4)
+    for w, r in zip(ids[:2], ref):
+        for x, y in zip(b.download(w), r):
+            assert np.array_equal(x, y)
+    assert b.counts()[0] == 3
+    b.close()
+
+
+def test_batch_matches_the_single_world_context(gpu):
+    """Same world through plg_step and through a batch: the same arithmetic."""
+    from plgpu.physics import GpuWorld
+
+    spec = uniform_world(25_000, 7, 0.017, seed=61, vel_scale=0.01)
+    w = GpuWorld(2, spec.n)
+    w.set_settings(spec.rmax, spec.friction, spec.force, spec.dt, beta=spec.beta, wrap=spec.wrap)
+    w.set_matrix(spec.matrix)
+    w.upload(spec.pos, spec.vel, spec.types)
+    w.step(5)
+    single = w.download()
+    w.close()
+    b, (_, wid) = make_batch(2, [uniform_world(3_000, 4, 0.05, seed=62), spec])
+    got = trajectory(b, wid, 5)
+    b.close()
+    assert np.array_equal(single[3], got[3])  # same order
+    np.testing.assert_allclose(got[0], single[0], rtol=0, atol=2e-7)
+    np.testing.assert_allclose(got[1], single[1], rtol=1e-5, atol=1e-9)
+
+
+def test_batch_rejects_what_it_cannot_run(gpu):
+    from plgpu import _lib
+
+    b, ids = make_batch(2, [uniform_world(1_000, 3, 0.05, seed=71)])
+    big = uniform_world(100, 3, 0.5, seed=72)  # nx = 2
+    with pytest.raises(_lib.PlgError) as e:
+        b.update(add=[desc(big)])
+    assert e.value.status == _lib.PLG_E_UNSUPPORTED
+    with pytest.raises(_lib.PlgError) as e:
+        b.update(remove=[12345])
+    assert e.value.status == _lib.PLG_E_INVALID_ARG
+    huge = uniform_world(10_000, 3, 0.05, seed=73)
+    with pytest.raises(_lib.PlgError) as e:
+        b.update(add=[desc(huge)] * 3)  # capacity 2 x 1001 particles
+    assert e.value.status == _lib.PLG_E_CAPACITY
+    assert b.counts()[0] == 1  # unchanged after the rejections
+    b.step(2)
+    b.close()

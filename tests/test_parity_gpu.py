@@ -18,44 +18,13 @@ at a zero of the force (the exact-rmax lattice), where it is ill-conditioned.
 import numpy as np
 import pytest
 
-from worlds import (FRICTION_T_HALF_0043, WorldSpec, accel_errors, blob_world, f32, min_image, norm_rel,
-                    run_gpu_debug, run_oracle_debug, uniform_world)
+from worlds import WorldSpec, blob_world, compare_with_oracle, f32, run_gpu_debug, uniform_world
 
 pytestmark = pytest.mark.gpu
 
-ACC_TOL = 1e-5
-VEL_TOL = 1e-5
-POS_ABS = 1.2e-7
-
-
 def check_step(spec: WorldSpec, gpu, exact_only=False, normwise=True):
-    g, (gpos, gvel, gtypes, gids) = run_gpu_debug(spec)
-    d, o = run_oracle_debug(spec)
-    assert np.array_equal(gids, o.ids), "sorted order (ids) differs from the oracle"
-    assert np.array_equal(gtypes, o.types)
-    assert np.array_equal(g["cell"], d["cell"]), "cell assignment differs"
-    assert np.array_equal(g["pairs"], d["pairs"]), "interacting-pair counts differ"
-    assert np.array_equal(g["hsum"], d["hsum"]), "interacting-pair sets differ (sum hash)"
-    assert np.array_equal(g["hxor"], d["hxor"]), "interacting-pair sets differ (xor hash)"
-    out = dict(pairs=float(d["pairs"].mean()) if spec.n else 0.0)
-    if spec.n == 0 or d["pairs"].sum() == 0 or exact_only:
-        return out
-    acc_g = g["acc"].astype(np.float64)
-    e = accel_errors(acc_g, d["acc"])
-    if normwise:
-        assert e["normwise"] <= ACC_TOL, e
-    scale = np.where(d["fscale"] > 0, d["fscale"], 1.0)
-    per = np.linalg.norm(acc_g - d["acc"], axis=1) / scale
-    assert per.max() <= ACC_TOL, per.max()
-    dim = spec.dim
-    if normwise:
-        assert norm_rel(gvel[:, :dim], o.vel[:, :dim]) <= VEL_TOL
-    dp = np.abs(min_image(gpos[:, :dim] - o.pos[:, :dim], spec.wrap))
-    dv = VEL_TOL * np.abs(o.vel[:, :dim]) + ACC_TOL * (spec.rmax * spec.force * spec.dt) * d["fscale"][:, None]
-    bound = POS_ABS + spec.dt * dv
-    assert np.all(dp <= bound), float((dp / bound).max())
-    out.update(e)
-    return out
+    g, state = run_gpu_debug(spec)
+    return compare_with_oracle(spec, g, state, exact_only=exact_only, normwise=normwise)
 
 
 def test_cfg1_2d_10k(gpu):

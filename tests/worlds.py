@@ -116,3 +116,40 @@ def accel_errors(acc_gpu: np.ndarray, acc_ref: np.ndarray, abs_terms: np.ndarray
     if raw.size:
         out.update(p50=float(np.percentile(raw, 50)), p99=float(np.percentile(raw, 99)), max=float(raw.max()))
     return out
+
+
+ACC_TOL = 1e-5
+VEL_TOL = 1e-5
+POS_ABS = 1.2e-7
+
+
+def compare_with_oracle(spec: WorldSpec, g: dict, state, exact_only=False, normwise=True):
+    """Asserts one GPU step (debug outputs `g`, downloaded `state`) against
+    the oracle's step of the same start state; returns error figures."""
+    gpos, gvel, gtypes, gids = state
+    d, o = run_oracle_debug(spec)
+    assert np.array_equal(gids, o.ids), "sorted order (ids) differs from the oracle"
+    assert np.array_equal(gtypes, o.types)
+    assert np.array_equal(g["cell"], d["cell"]), "cell assignment differs"
+    assert np.array_equal(g["pairs"], d["pairs"]), "interacting-pair counts differ"
+    assert np.array_equal(g["hsum"], d["hsum"]), "interacting-pair sets differ (sum hash)"
+    assert np.array_equal(g["hxor"], d["hxor"]), "interacting-pair sets differ (xor hash)"
+    out = dict(pairs=float(d["pairs"].mean()) if spec.n else 0.0)
+    if spec.n == 0 or d["pairs"].sum() == 0 or exact_only:
+        return out
+    acc_g = g["acc"].astype(np.float64)
+    e = accel_errors(acc_g, d["acc"])
+    if normwise:
+        assert e["normwise"] <= ACC_TOL, e
+    scale = np.where(d["fscale"] > 0, d["fscale"], 1.0)
+    per = np.linalg.norm(acc_g - d["acc"], axis=1) / scale
+    assert per.max() <= ACC_TOL, per.max()
+    dim = spec.dim
+    if normwise:
+        assert norm_rel(gvel[:, :dim], o.vel[:, :dim]) <= VEL_TOL
+    dp = np.abs(min_image(gpos[:, :dim] - o.pos[:, :dim], spec.wrap))
+    dv = VEL_TOL * np.abs(o.vel[:, :dim]) + ACC_TOL * (spec.rmax * spec.force * spec.dt) * d["fscale"][:, None]
+    bound = POS_ABS + spec.dt * dv
+    assert np.all(dp <= bound), float((dp / bound).max())
+    out.update(e)
+    return out
