@@ -247,6 +247,19 @@ int plg_batch_set_use_graph(plg_batch* batch, int32_t on);
 int plg_batch_get_stream(plg_batch* batch, void** stream);
 const char* plg_batch_last_error(plg_batch* batch);
 int plg_batch_step_stats(plg_batch* batch, int64_t* deferred);
+/* Force kernel tile variants (threads = targets per block, staging size):
+ * 0 = large tiles for dense worlds, 1 = small tiles for sparse worlds.  The
+ * cell size is not a tuning choice: it is rmax (the sorted order the
+ * reference exposes depends on it). */
+#define PLG_TILE_VARIANTS 2
+int plg_batch_set_tile(plg_batch* batch, int32_t variant);
+int plg_batch_get_tile(plg_batch* batch, int32_t* variant);
+/* Autotuner: times `steps` steps of every tile variant on the batch as it
+ * is (restoring the particle state after each trial, so no world moves),
+ * keeps the fastest and reports it; ms_per_step (may be NULL) receives
+ * PLG_TILE_VARIANTS times.  Allocates a temporary copy of the state. */
+int plg_batch_autotune(plg_batch* batch, int32_t steps, int32_t* chosen, double* ms_per_step);
+
 /* plg_debug_step over the whole batch: per sorted slot (worlds one after
  * another), cell = global cell index (world's first cell + its own). */
 int plg_batch_debug_step(plg_batch* batch, int32_t* cell, int32_t* pairs,

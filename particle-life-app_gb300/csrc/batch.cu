@@ -89,6 +89,7 @@ struct plg_batch {
 
     std::vector<WorldRec> worlds;  // device order
     int32_t next_id = 1;
+    int variant = 0;  // force kernel tile variant (autotuner)
     int64_t n_total = 0, c_total = 0;
     bool smem_matrix = true;
 
@@ -391,7 +392,7 @@ void enqueue_batch_step(plg_batch* b, const DebugOut* dbg, int32_t* cell_sorted)
                      sbuf<D>(b->bpt, b->bvel, 0), cell_sorted);
     launch_force_batch<D>(st, b->worlds_d, b->wp_off_d, (int)b->worlds.size(), n, b->smem_matrix,
                           sbuf<D>(b->bpt, b->bvel, 0), b->cstart, sbuf<D>(b->apt, b->avel, 0), b->cell, b->rank,
-                          b->counts, b->defer, dbg);
+                          b->counts, b->defer, dbg, b->variant);
 }
 
 int enqueue_step(plg_batch* b) {
@@ -602,6 +603,95 @@ int plg_batch_download(plg_batch* b, int32_t id, double* pos, double* vel, int32
     if (type && !mtype) BCK(b, cudaMemcpyAsync(type, stype, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, st));
     if (pid && !mid) BCK(b, cudaMemcpyAsync(pid, sid, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, st));
     BCK(b, cudaStreamSynchronize(st));
+    return PLG_OK;
+}
+
+int plg_batch_set_tile(plg_batch* b, int32_t variant) {
+    if (!b) return PLG_E_INVALID_ARG;
+    if (variant < 0 || variant >= PLG_TILE_VARIANTS) return berr(b, PLG_E_INVALID_ARG, "unknown tile variant");
+    if (variant != b->variant) destroy_batch_graph(b);
+    b->variant = variant;
+    return PLG_OK;
+}
+
+int plg_batch_get_tile(plg_batch* b, int32_t* variant) {
+    if (!b || !variant) return PLG_E_INVALID_ARG;
+    *variant = b->variant;
+    return PLG_OK;
+}
+
+// Times `steps` steps of each tile variant on the batch as it is, restoring
+// the particle state after each trial, and keeps the fastest variant.  The
+// trials allocate a copy of the state and free it before returning.
+int plg_batch_autotune(plg_batch* b, int32_t steps, int32_t* chosen, double* ms_per_step) {
+    if (!b) return PLG_E_INVALID_ARG;
+    if (steps < 1) return berr(b, PLG_E_INVALID_ARG, "autotune needs at least one step");
+    BatchDeviceGuard g(b->device);
+    cudaStream_t st = b->stream;
+    const size_t n = (size_t)b->n_total, nc = (size_t)std::max<int64_t>(b->c_total, 1);
+    if (n == 0) {
+        if (chosen) *chosen = b->variant;
+        return PLG_OK;
+    }
+    const size_t vel_sz = b->dim == 2 ? sizeof(float2) : sizeof(float4);
+    const size_t bytes[5] = {sizeof(float4) * n, vel_sz * n, 4 * n, 4 * n, 4 * nc};
+    void* live[5] = {b->apt, b->avel, b->cell, b->rank, b->counts};
+    void* save[5] = {};
+    int rc = PLG_OK;
+    for (int k = 0; k < 5 && !rc; ++k)
+        if (cudaMalloc(&save[k], bytes[k]) != cudaSuccess) {
+            cudaGetLastError();
+            rc = berr(b, PLG_E_NO_MEMORY, "cudaMalloc (autotune state copy)");
+        }
+    auto copy_all = [&](bool restore) -> cudaError_t {
+        for (int k = 0; k < 5; ++k) {
+            // A and B swap only in plg_batch_update, so `live` stays valid.
+            cudaError_t e = cudaMemcpyAsync(restore ? live[k] : save[k], restore ? save[k] : live[k], bytes[k],
+                                            cudaMemcpyDeviceToDevice, st);
+            if (e != cudaSuccess) return e;
+        }
+        return cudaSuccess;
+    };
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (!rc && (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)) rc = PLG_E_CUDA;
+    if (!rc && copy_all(false) != cudaSuccess) rc = bcuda(b, "autotune save", cudaGetLastError());
+    const int old = b->variant;
+    double best = 1e300;
+    int best_v = old;
+    for (int v = 0; v < PLG_TILE_VARIANTS && !rc; ++v) {
+        if (v != b->variant) destroy_batch_graph(b);
+        b->variant = v;
+        if ((rc = enqueue_step(b))) break;  // builds the graph, untimed
+        if (cudaEventRecord(e0, st) != cudaSuccess) rc = PLG_E_CUDA;
+        for (int32_t k = 0; k < steps && !rc; ++k) rc = enqueue_step(b);
+        if (rc) break;
+        float ms = 0.f;
+        if (cudaEventRecord(e1, st) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
+            cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) {
+            rc = bcuda(b, "autotune timing", cudaGetLastError());
+            break;
+        }
+        const double per = ms / steps;
+        if (ms_per_step) ms_per_step[v] = per;
+        if (per < best) {
+            best = per;
+            best_v = v;
+        }
+        if (copy_all(true) != cudaSuccess) rc = bcuda(b, "autotune restore", cudaGetLastError());
+    }
+    if (!rc && cudaStreamSynchronize(st) != cudaSuccess) rc = bcuda(b, "autotune", cudaGetLastError());
+    for (void* p : save)
+        if (p) cudaFree(p);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (rc) {
+        b->variant = old;
+        destroy_batch_graph(b);
+        return rc;
+    }
+    if (best_v != b->variant) destroy_batch_graph(b);
+    b->variant = best_v;
+    if (chosen) *chosen = best_v;
     return PLG_OK;
 }
 

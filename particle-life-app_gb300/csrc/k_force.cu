@@ -438,12 +438,30 @@ struct TileRows {
     static constexpr int R = D == 3 ? 9 : 3;
 };
 
-template <int D>
-struct TileCfg {
-    static constexpr int kTargets = D == 3 ? 128 : 256;  // targets per block, one thread each
-    static constexpr int kMinBlocks = D == 3 ? 4 : 6;    // resident blocks per SM the smem allows
-    static constexpr int kCap = D == 3 ? 2560 : 1536;    // staged candidates per segment
-    static constexpr int kCells = 512;                   // stencil cells per segment (R x columns)
+// Tile variants (the autotuner's choice, PLG_TILE_*):
+//   kTargets    targets per block, one thread each
+//   kMinBlocks  resident blocks per SM the shared memory allows (caps registers)
+//   kCap        staged candidates per segment
+//   kCells      stencil cells per segment (R x columns)
+// Variant 0 suits dense worlds; variant 1 (smaller tiles, less shared memory,
+// more resident blocks) suits sparse ones, where a tile spans many rows.
+template <int D, int V>
+struct TileCfg;
+template <>
+struct TileCfg<2, 0> {
+    static constexpr int kTargets = 256, kMinBlocks = 6, kCap = 1536, kCells = 512;
+};
+template <>
+struct TileCfg<2, 1> {
+    static constexpr int kTargets = 128, kMinBlocks = 8, kCap = 1024, kCells = 512;
+};
+template <>
+struct TileCfg<3, 0> {
+    static constexpr int kTargets = 128, kMinBlocks = 4, kCap = 2560, kCells = 512;
+};
+template <>
+struct TileCfg<3, 1> {
+    static constexpr int kTargets = 128, kMinBlocks = 5, kCap = 1280, kCells = 512;
 };
 
 // Target shifts a staged candidate asks for (bits 16..18 of its type word):
@@ -451,16 +469,16 @@ struct TileCfg {
 // the periodic image above the box of a cell near coordinate 0.
 constexpr int kShiftX = 1 << 16, kShiftY = 1 << 17, kShiftZ = 1 << 18;
 
-// Lives in dynamic shared memory (about 31 KB in 2D, 47 KB in 3D).
-template <int D>
+// Lives in dynamic shared memory (variant 0: about 31 KB in 2D, 47 KB in 3D).
+template <int D, int V>
 struct TileSmem {
-    float4 cand[TileCfg<D>::kCap];      // staged candidates, column-major by stencil cell
-    int coff[TileCfg<D>::kCells + 1];   // smem start of stencil cell e = column * R + row
-    int cglob[TileCfg<D>::kCells];      // sorted-order start of stencil cell e
-    int rowid[TileCfg<D>::kTargets];
-    int colid[TileCfg<D>::kTargets];
-    int seg[TileCfg<D>::kTargets + 1];
-    int wsum[TileCfg<D>::kTargets / 32];
+    float4 cand[TileCfg<D, V>::kCap];      // staged candidates, column-major by stencil cell
+    int coff[TileCfg<D, V>::kCells + 1];   // smem start of stencil cell e = column * R + row
+    int cglob[TileCfg<D, V>::kCells];      // sorted-order start of stencil cell e
+    int rowid[TileCfg<D, V>::kTargets];
+    int colid[TileCfg<D, V>::kTargets];
+    int seg[TileCfg<D, V>::kTargets + 1];
+    int wsum[TileCfg<D, V>::kTargets / 32];
     int nseg;
     int staged;                         // 1: the segment's stencil is in smem
     float mat[kSmemMatrixMax * kSmemMatrixMax];
@@ -469,10 +487,10 @@ struct TileSmem {
 __device__ __forceinline__ int wrap_index(int c, int n) { return c < 0 ? c + n : (c >= n ? c - n : c); }
 
 // Block-wide exclusive scan of v[0..n) in place (n <= kCells); returns the total.
-template <int D>
+template <int D, int V>
 __device__ __forceinline__ int block_scan_inplace(int* v, int n, int* wsum) {
-    constexpr int kT = TileCfg<D>::kTargets;
-    constexpr int per = (TileCfg<D>::kCells + kT - 1) / kT;
+    constexpr int kT = TileCfg<D, V>::kTargets;
+    constexpr int per = (TileCfg<D, V>::kCells + kT - 1) / kT;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     int loc[per];
     int sum = 0;
@@ -514,9 +532,9 @@ __device__ __forceinline__ int block_scan_inplace(int* v, int n, int* wsum) {
 // the single contiguous range of columns cx-1 .. cx+1.  Images below the box
 // are shifted down by 1 here (exact: their coordinates are >= 0.5); images
 // above it are flagged for a target shift instead.
-template <int D>
+template <int D, int V>
 __device__ __forceinline__ void stage_segment(const ForceArgs<D>& A, const ForceParams& P,
-                                              const uint32_t* __restrict__ cs, TileSmem<D>& sm, int srow, int cxa,
+                                              const uint32_t* __restrict__ cs, TileSmem<D, V>& sm, int srow, int cxa,
                                               int cxb) {
     constexpr int R = TileRows<D>::R;
     const int nx = P.g.nx;
@@ -524,12 +542,12 @@ __device__ __forceinline__ void stage_segment(const ForceArgs<D>& A, const Force
     const int cy = D == 3 ? srow % nx : srow, cz = D == 3 ? srow / nx : 0;
     const int ncols = cxb - cxa + 1;
     const int ncell = R * (ncols + 2);
-    if (ncell > TileCfg<D>::kCells) {
+    if (ncell > TileCfg<D, V>::kCells) {
         if (tid == 0) sm.staged = 0;
         __syncthreads();
         return;
     }
-    for (int e = tid; e < ncell; e += TileCfg<D>::kTargets) {
+    for (int e = tid; e < ncell; e += TileCfg<D, V>::kTargets) {
         const int ci = e / R, r = e - ci * R;
         const int col = wrap_index(cxa - 1 + ci, nx);
         const int ry = wrap_index(cy + r % 3 - 1, nx);
@@ -540,14 +558,14 @@ __device__ __forceinline__ void stage_segment(const ForceArgs<D>& A, const Force
         sm.coff[e] = (int)__ldg(cs + c + 1) - g0;
     }
     __syncthreads();
-    const int total = block_scan_inplace<D>(sm.coff, ncell, sm.wsum);
+    const int total = block_scan_inplace<D, V>(sm.coff, ncell, sm.wsum);
     if (tid == 0) {
         sm.coff[ncell] = total;
-        sm.staged = total <= TileCfg<D>::kCap;
+        sm.staged = total <= TileCfg<D, V>::kCap;
     }
     __syncthreads();
     if (!sm.staged) return;
-    for (int k = tid; k < total; k += TileCfg<D>::kTargets) {
+    for (int k = tid; k < total; k += TileCfg<D, V>::kTargets) {
         int lo = 0, hi = ncell;  // last e with coff[e] <= k
         while (hi - lo > 1) {
             const int m = (lo + hi) >> 1;
@@ -582,8 +600,8 @@ __device__ __forceinline__ void stage_segment(const ForceArgs<D>& A, const Force
 }
 
 // Global sorted slot of staged candidate j (rare path and debug only).
-template <int D>
-__device__ __forceinline__ int staged_global(const TileSmem<D>& sm, int ncell, int j) {
+template <int D, int V>
+__device__ __forceinline__ int staged_global(const TileSmem<D, V>& sm, int ncell, int j) {
     int lo = 0, hi = ncell;
     while (hi - lo > 1) {
         const int m = (lo + hi) >> 1;
@@ -612,8 +630,8 @@ __device__ __forceinline__ float rsqrt_approx(float x) {
 // true: the caller then defers the target to the FP64 fixup, which discards
 // this partial sum.  SHIFT: the segment touches the box's upper boundary,
 // so some candidates carry target-shift flags.
-template <int D, bool DBG, bool SHIFT>
-__device__ __forceinline__ bool tile_range(const ForceArgs<D>& A, const ForceParams& P, const TileSmem<D>& sm,
+template <int D, bool DBG, bool SHIFT, int V>
+__device__ __forceinline__ bool tile_range(const ForceArgs<D>& A, const ForceParams& P, const TileSmem<D, V>& sm,
                                            const float* __restrict__ Mrow, int ncell, int ja, int jb, float px,
                                            float py, float pz, Acc& acc) {
     const float px1 = px - 1.f, py1 = py - 1.f, pz1 = pz - 1.f;
@@ -713,13 +731,13 @@ constexpr int kRowMask = (1 << kRowBits) - 1;
 // are disjoint ranges of one global cell index); each target finds its
 // world's parameters in A.worlds, and segments never mix worlds, so every
 // target computes exactly what a single-world launch would.
-template <int D, bool DBG, bool SMEM_M, bool BATCH>
-__global__ void __launch_bounds__(TileCfg<D>::kTargets, TileCfg<D>::kMinBlocks)
+template <int D, bool DBG, bool SMEM_M, bool BATCH, int V>
+__global__ void __launch_bounds__(TileCfg<D, V>::kTargets, TileCfg<D, V>::kMinBlocks)
     k_force_tile(const __grid_constant__ ForceArgs<D> A) {
-    constexpr int kT = TileCfg<D>::kTargets;
+    constexpr int kT = TileCfg<D, V>::kTargets;
     constexpr int R = TileRows<D>::R;
     extern __shared__ __align__(16) unsigned char smraw[];
-    TileSmem<D>& sm = *reinterpret_cast<TileSmem<D>*>(smraw);
+    TileSmem<D, V>& sm = *reinterpret_cast<TileSmem<D, V>*>(smraw);
     const int tid = threadIdx.x;
     const int ntot = BATCH ? A.n_total : A.p.n;
     const int s0 = blockIdx.x * kT;
@@ -780,7 +798,7 @@ __global__ void __launch_bounds__(TileCfg<D>::kTargets, TileCfg<D>::kMinBlocks)
             const int nn = SP.ntypes * SP.ntypes;
             for (int k = tid; k < nn; k += kT) sm.mat[k] = SP.matrix[k];
         }
-        stage_segment<D>(A, SP, A.cstart + SP.cell_base, sm, srow, cxa, cxb);
+        stage_segment<D, V>(A, SP, A.cstart + SP.cell_base, sm, srow, cxa, cxb);
         if (tid >= ta && tid < tb) {
             if (sm.staged) {
                 const int nx = P.g.nx;
@@ -793,11 +811,11 @@ __global__ void __launch_bounds__(TileCfg<D>::kTargets, TileCfg<D>::kMinBlocks)
                 const bool shift = P.wrap && (cxb == nx - 1 || cy == nx - 1 || (D == 3 && cz == nx - 1));
                 // The target itself splits its run: [j0, self_j) and (self_j, j1).
                 if (shift) {
-                    defer = tile_range<D, DBG, true>(A, P, sm, Mrow, ncell, j0, self_j, px, py, pz, acc);
-                    defer |= tile_range<D, DBG, true>(A, P, sm, Mrow, ncell, self_j + 1, j1, px, py, pz, acc);
+                    defer = tile_range<D, DBG, true, V>(A, P, sm, Mrow, ncell, j0, self_j, px, py, pz, acc);
+                    defer |= tile_range<D, DBG, true, V>(A, P, sm, Mrow, ncell, self_j + 1, j1, px, py, pz, acc);
                 } else {
-                    defer = tile_range<D, DBG, false>(A, P, sm, Mrow, ncell, j0, self_j, px, py, pz, acc);
-                    defer |= tile_range<D, DBG, false>(A, P, sm, Mrow, ncell, self_j + 1, j1, px, py, pz, acc);
+                    defer = tile_range<D, DBG, false, V>(A, P, sm, Mrow, ncell, j0, self_j, px, py, pz, acc);
+                    defer |= tile_range<D, DBG, false, V>(A, P, sm, Mrow, ncell, self_j + 1, j1, px, py, pz, acc);
                 }
             } else {
                 defer = true;
@@ -843,8 +861,27 @@ __global__ void __launch_bounds__(TileCfg<D>::kTargets, TileCfg<D>::kMinBlocks)
     }
 }
 
+template <int D, bool DBG, bool BATCH, int V>
+void launch_tile(cudaStream_t st, const ForceArgs<D>& A, bool smem_matrix) {
+    constexpr int kT = TileCfg<D, V>::kTargets;
+    const int grid = (A.n_total + kT - 1) / kT;
+    const size_t sb = sizeof(TileSmem<D, V>);
+    if (smem_matrix)
+        k_force_tile<D, DBG, true, BATCH, V><<<grid, kT, sb, st>>>(A);
+    else
+        k_force_tile<D, DBG, false, BATCH, V><<<grid, kT, sb, st>>>(A);
+}
+
+template <int D, bool DBG, bool BATCH>
+void launch_tile_variant(cudaStream_t st, const ForceArgs<D>& A, bool smem_matrix, int variant) {
+    if (variant == 1)
+        launch_tile<D, DBG, BATCH, 1>(st, A, smem_matrix);
+    else
+        launch_tile<D, DBG, BATCH, 0>(st, A, smem_matrix);
+}
+
 template <int D, bool DBG>
-void launch_variant(cudaStream_t st, const ForceArgs<D>& A, bool general) {
+void launch_variant(cudaStream_t st, const ForceArgs<D>& A, bool general, int variant) {
     const int n = A.p.n;
     const bool smem = A.p.ntypes <= kSmemMatrixMax;
     if (general) {
@@ -855,13 +892,7 @@ void launch_variant(cudaStream_t st, const ForceArgs<D>& A, bool general) {
         else
             k_force_general<D, DBG, false><<<grid, kThreads, 0, st>>>(A);
     } else {
-        constexpr int kT = TileCfg<D>::kTargets;
-        const int grid = (n + kT - 1) / kT;
-        const size_t sb = sizeof(TileSmem<D>);
-        if (smem)
-            k_force_tile<D, DBG, true, false><<<grid, kT, sb, st>>>(A);
-        else
-            k_force_tile<D, DBG, false, false><<<grid, kT, sb, st>>>(A);
+        launch_tile_variant<D, DBG, false>(st, A, smem, variant);
     }
 }
 
@@ -892,19 +923,19 @@ ForceArgs<D> make_args(const ForceParams& p, StateBuf<D> b, const uint32_t* csta
 template <int D>
 void launch_force(cudaStream_t st, const ForceParams& p, bool general, StateBuf<D> b, const uint32_t* cstart,
                   StateBuf<D> a, uint32_t* cell, uint32_t* rank, uint32_t* counts, uint32_t* defer,
-                  const DebugOut* dbg) {
+                  const DebugOut* dbg, int variant) {
     if (p.n <= 0) return;
     const ForceArgs<D> A = make_args<D>(p, b, cstart, a, cell, rank, counts, defer, dbg);
     if (dbg)
-        launch_variant<D, true>(st, A, general);
+        launch_variant<D, true>(st, A, general, variant);
     else
-        launch_variant<D, false>(st, A, general);
+        launch_variant<D, false>(st, A, general, variant);
 }
 
 template <int D>
 void launch_force_batch(cudaStream_t st, const ForceParams* worlds, const int* wp_off, int nworlds, int n_total,
                         bool smem_matrix, StateBuf<D> b, const uint32_t* cstart, StateBuf<D> a, uint32_t* cell,
-                        uint32_t* rank, uint32_t* counts, uint32_t* defer, const DebugOut* dbg) {
+                        uint32_t* rank, uint32_t* counts, uint32_t* defer, const DebugOut* dbg, int variant) {
     if (n_total <= 0 || nworlds <= 0) return;
     ForceParams none{};
     ForceArgs<D> A = make_args<D>(none, b, cstart, a, cell, rank, counts, defer, dbg);
@@ -912,54 +943,46 @@ void launch_force_batch(cudaStream_t st, const ForceParams* worlds, const int* w
     A.wp_off = wp_off;
     A.nworlds = nworlds;
     A.n_total = n_total;
-    constexpr int kT = TileCfg<D>::kTargets;
-    const int grid = (n_total + kT - 1) / kT;
-    const size_t sb = sizeof(TileSmem<D>);
-    if (dbg) {
-        if (smem_matrix)
-            k_force_tile<D, true, true, true><<<grid, kT, sb, st>>>(A);
-        else
-            k_force_tile<D, true, false, true><<<grid, kT, sb, st>>>(A);
-    } else {
-        if (smem_matrix)
-            k_force_tile<D, false, true, true><<<grid, kT, sb, st>>>(A);
-        else
-            k_force_tile<D, false, false, true><<<grid, kT, sb, st>>>(A);
-    }
+    if (dbg)
+        launch_tile_variant<D, true, true>(st, A, smem_matrix, variant);
+    else
+        launch_tile_variant<D, false, true>(st, A, smem_matrix, variant);
 }
 
 template void launch_force_batch<2>(cudaStream_t, const ForceParams*, const int*, int, int, bool, StateBuf<2>,
                                     const uint32_t*, StateBuf<2>, uint32_t*, uint32_t*, uint32_t*, uint32_t*,
-                                    const DebugOut*);
+                                    const DebugOut*, int);
 template void launch_force_batch<3>(cudaStream_t, const ForceParams*, const int*, int, int, bool, StateBuf<3>,
                                     const uint32_t*, StateBuf<3>, uint32_t*, uint32_t*, uint32_t*, uint32_t*,
-                                    const DebugOut*);
+                                    const DebugOut*, int);
 
 template void launch_force<2>(cudaStream_t, const ForceParams&, bool, StateBuf<2>, const uint32_t*, StateBuf<2>,
-                              uint32_t*, uint32_t*, uint32_t*, uint32_t*, const DebugOut*);
+                              uint32_t*, uint32_t*, uint32_t*, uint32_t*, const DebugOut*, int);
 template void launch_force<3>(cudaStream_t, const ForceParams&, bool, StateBuf<3>, const uint32_t*, StateBuf<3>,
-                              uint32_t*, uint32_t*, uint32_t*, uint32_t*, const DebugOut*);
+                              uint32_t*, uint32_t*, uint32_t*, uint32_t*, const DebugOut*, int);
 
-template <int D, bool DBG, bool SMEM_M, bool BATCH>
+template <int D, bool DBG, bool SMEM_M, bool BATCH, int V>
 cudaError_t allow_one() {
-    return cudaFuncSetAttribute(k_force_tile<D, DBG, SMEM_M, BATCH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)sizeof(TileSmem<D>));
+    return cudaFuncSetAttribute(k_force_tile<D, DBG, SMEM_M, BATCH, V>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)sizeof(TileSmem<D, V>));
 }
 
-template <int D>
+template <int D, int V>
 cudaError_t allow_tile_smem() {
-    const cudaError_t es[] = {allow_one<D, false, true, false>(), allow_one<D, false, false, false>(),
-                              allow_one<D, true, true, false>(),  allow_one<D, true, false, false>(),
-                              allow_one<D, false, true, true>(),  allow_one<D, false, false, true>(),
-                              allow_one<D, true, true, true>(),   allow_one<D, true, false, true>()};
+    const cudaError_t es[] = {allow_one<D, false, true, false, V>(), allow_one<D, false, false, false, V>(),
+                              allow_one<D, true, true, false, V>(),  allow_one<D, true, false, false, V>(),
+                              allow_one<D, false, true, true, V>(),  allow_one<D, false, false, true, V>(),
+                              allow_one<D, true, true, true, V>(),   allow_one<D, true, false, true, V>()};
     for (cudaError_t e : es)
         if (e != cudaSuccess) return e;
     return cudaSuccess;
 }
 
 cudaError_t force_kernels_init() {
-    cudaError_t e = allow_tile_smem<2>();
-    if (e == cudaSuccess) e = allow_tile_smem<3>();
+    cudaError_t e = allow_tile_smem<2, 0>();
+    if (e == cudaSuccess) e = allow_tile_smem<2, 1>();
+    if (e == cudaSuccess) e = allow_tile_smem<3, 0>();
+    if (e == cudaSuccess) e = allow_tile_smem<3, 1>();
     return e;
 }
 

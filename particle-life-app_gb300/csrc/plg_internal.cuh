@@ -197,10 +197,11 @@ void launch_gather(cudaStream_t st, int n, const uint32_t* perm, const uint32_t*
 
 // `defer`: one word, zeroed before the step; counts the targets the tiled
 // kernel recomputed in its deferred pass.
+// variant: tile variant of the force kernel (0 or 1, the autotuner's knob).
 template <int D>
 void launch_force(cudaStream_t st, const ForceParams& p, bool general, StateBuf<D> b, const uint32_t* cstart,
                   StateBuf<D> a, uint32_t* cell, uint32_t* rank, uint32_t* counts, uint32_t* defer,
-                  const DebugOut* dbg);
+                  const DebugOut* dbg, int variant = 0);
 
 // Batched worlds: `worlds` (device, nworlds entries) holds each world's
 // parameters with its cell_base and p_off; `wp_off` (device, nworlds + 1)
@@ -209,7 +210,7 @@ void launch_force(cudaStream_t st, const ForceParams& p, bool general, StateBuf<
 template <int D>
 void launch_force_batch(cudaStream_t st, const ForceParams* worlds, const int* wp_off, int nworlds, int n_total,
                         bool smem_matrix, StateBuf<D> b, const uint32_t* cstart, StateBuf<D> a, uint32_t* cell,
-                        uint32_t* rank, uint32_t* counts, uint32_t* defer, const DebugOut* dbg);
+                        uint32_t* rank, uint32_t* counts, uint32_t* defer, const DebugOut* dbg, int variant = 0);
 
 // Opts the tiled force kernel in to its dynamic shared memory (> 48 KB) on
 // the current device; called once per context.

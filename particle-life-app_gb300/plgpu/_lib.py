@@ -25,6 +25,7 @@ PLG_E_DEVICE = 8
 PLG_E_CAPACITY = 9
 
 PLG_ACCEL_PARTICLE_LIFE = 1
+PLG_TILE_VARIANTS = 2
 PLG_NOALLOC_MAX_PARTICLES = 1 << 18
 PLG_NOALLOC_MAX_CELLS = 1 << 18
 
@@ -112,6 +113,9 @@ SIGNATURES = {
     "plg_batch_last_error": (C.c_char_p, [_P]),
     "plg_batch_step_stats": (C.c_int, [_P, _I64P]),
     "plg_batch_debug_step": (C.c_int, [_P, _I32P, _I32P, _U64P, _U64P, _FP, _I64P]),
+    "plg_batch_set_tile": (C.c_int, [_P, C.c_int32]),
+    "plg_batch_get_tile": (C.c_int, [_P, _I32P]),
+    "plg_batch_autotune": (C.c_int, [_P, C.c_int32, _I32P, _DP]),
 }
 
 _lib = None

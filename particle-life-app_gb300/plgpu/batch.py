@@ -137,6 +137,22 @@ class GpuBatch:
         out["cell"] = out["cell"] - c
         return out
 
+    def set_tile(self, variant: int) -> None:
+        _check(self.lib.plg_batch_set_tile(self.b, variant), self.b, "plg_batch_set_tile")
+
+    def tile(self) -> int:
+        v = _lib.C.c_int32()
+        _check(self.lib.plg_batch_get_tile(self.b, _lib.C.byref(v)), self.b, "plg_batch_get_tile")
+        return v.value
+
+    def autotune(self, steps: int = 3) -> tuple[int, list[float]]:
+        """Times every tile variant on the current batch (state restored) and
+        keeps the fastest; returns (variant, ms per step of each)."""
+        chosen = _lib.C.c_int32()
+        ms = (_lib.C.c_double * _lib.PLG_TILE_VARIANTS)()
+        _check(self.lib.plg_batch_autotune(self.b, steps, _lib.C.byref(chosen), ms), self.b, "plg_batch_autotune")
+        return chosen.value, list(ms)
+
     def deferred(self) -> int:
         v = _lib.C.c_int64()
         _check(self.lib.plg_batch_step_stats(self.b, _lib.C.byref(v)), self.b, "plg_batch_step_stats")

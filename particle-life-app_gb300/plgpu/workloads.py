@@ -1,0 +1,48 @@
+"""Seeded synthetic workloads for the batched and served forms.
+
+Reference units are the unit box [0,1)^d; a config quoted in a [-1,1]^d box
+has its lengths halved here.  Generators use numpy's Philox4x32
+counter-based PRNG (Salmon et al. 2011), so a seed fixes every world.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+from .batch import WorldDesc
+
+
+def friction_of_half_life(t_half: float) -> float:
+    """Per-1/60 s velocity factor whose pow(f, 60 t) halves in t_half seconds."""
+    return 0.5 ** (1.0 / (60.0 * t_half))
+
+
+def random_world(rng: np.random.Generator, dim: int, n: int, ntypes: int, rmax: float, friction: float,
+                 dt: float) -> WorldDesc:
+    pos = np.zeros((n, 3))
+    pos[:, :dim] = rng.random((n, dim), dtype=np.float32)
+    types = rng.integers(0, ntypes, n).astype(np.int32)
+    m = np.asarray(2 * rng.random((ntypes, ntypes)) - 1, np.float32).astype(np.float64)
+    return WorldDesc(pos=pos, types=types, matrix=m, rmax=rmax, friction=friction, dt=dt)
+
+
+def batched_worlds(count: int = 512, seed: int = 7, n_lo: int = 1_000, n_hi: int = 200_000) -> list[WorldDesc]:
+    """The batched configuration: `count` 2D periodic worlds, N log-uniform in
+    [n_lo, n_hi], types uniform in 3..12, matrix uniform in [-1,1], rmax
+    uniform in [0.01, 0.06] of a [-1,1]^2 box (0.005..0.03 here), friction
+    half-life uniform in [0.02, 0.1] s, dt = 0.02, positions uniform,
+    velocities zero."""
+    rng = np.random.Generator(np.random.Philox(seed))
+    out = []
+    for _ in range(count):
+        n = int(round(math.exp(rng.uniform(math.log(n_lo), math.log(n_hi)))))
+        ntypes = int(rng.integers(3, 13))
+        rmax = float(rng.uniform(0.01, 0.06)) / 2
+        friction = friction_of_half_life(float(rng.uniform(0.02, 0.1)))
+        out.append(random_world(rng, 2, n, ntypes, rmax, friction, 0.02))
+    return out
+
+
+def cells_of(w: WorldDesc, dim: int) -> int:
+    return int(math.floor(1.0 / w.rmax)) ** dim

@@ -37,9 +37,11 @@ def mixed_2d_specs():
     ]
 
 
-def test_batch_2d_every_world_matches_the_oracle(gpu):
+@pytest.mark.parametrize("variant", [0, 1])
+def test_batch_2d_every_world_matches_the_oracle(gpu, variant):
     specs = mixed_2d_specs()
     b, ids = make_batch(2, specs)
+    b.set_tile(variant)
     dbg = b.debug_step()
     for spec, wid in zip(specs, ids):
         g = b.world_debug(dbg, wid)
@@ -47,13 +49,15 @@ def test_batch_2d_every_world_matches_the_oracle(gpu):
     b.close()
 
 
-def test_batch_3d_every_world_matches_the_oracle(gpu):
+@pytest.mark.parametrize("variant", [0, 1])
+def test_batch_3d_every_world_matches_the_oracle(gpu, variant):
     specs = [
         uniform_world(40_000, 8, 0.04, seed=51, dim=3, vel_scale=0.01, dt=0.01),
         blob_world(30_000, 16, 0.02, nblobs=6, sigma=0.02, seed=52, dim=3),
         uniform_world(2_000, 3, 0.26, seed=53, dim=3),
     ]
     b, ids = make_batch(3, specs)
+    b.set_tile(variant)
     dbg = b.debug_step()
     for spec, wid in zip(specs, ids):
         compare_with_oracle(spec, b.world_debug(dbg, wid), b.download(wid))
@@ -137,3 +141,26 @@ def test_batch_rejects_what_it_cannot_run(gpu):
     assert b.counts()[0] == 1  # unchanged after the rejections
     b.step(2)
     b.close()
+
+
+def test_autotune_restores_state_and_variants_agree(gpu):
+    specs = mixed_2d_specs()[:4]
+    b, ids = make_batch(2, specs)
+    b.step(2)
+    before = [b.download(w) for w in ids]
+    v, ms = b.autotune(2)
+    assert v == b.tile() and v in (0, 1) and all(m > 0 for m in ms)
+    for w, ref in zip(ids, before):
+        for x, y in zip(b.download(w), ref):
+            assert np.array_equal(x, y)
+    b.close()
+    runs = []
+    for variant in (0, 1):
+        bb, ii = make_batch(2, specs)
+        bb.set_tile(variant)
+        bb.step(4)
+        runs.append([bb.download(w) for w in ii])
+        bb.close()
+    for r0, r1 in zip(*runs):
+        assert np.array_equal(r0[3], r1[3])
+        np.testing.assert_allclose(r0[0], r1[0], rtol=0, atol=1e-6)
