@@ -70,6 +70,8 @@ struct plg_batch {
 
     ForceParams* worlds_d = nullptr;  // wcap
     int* wp_off_d = nullptr;          // wcap + 1
+    int* tile_off_d = nullptr;        // PLG_TILE_VARIANTS x (wcap + 1): first tile of each world
+    int tiles[PLG_TILE_VARIANTS] = {};
     int* move_new_d = nullptr;        // wcap + 1
     int* move_old_d = nullptr;        // wcap
     float* bounds_d = nullptr;
@@ -179,6 +181,7 @@ void free_batch(plg_batch* b) {
     void* ptrs[] = {b->apt,      b->bpt,       b->avel,      b->bvel,        b->cell,     b->rank,
                     b->perm,     b->slot_cell, b->counts,    b->cstart,      b->scan_state, b->defer,
                     b->status_d, b->worlds_d,  b->wp_off_d,  b->move_new_d,  b->move_old_d, b->bounds_d,
+                    b->tile_off_d,
                     b->matrix_d, b->stage,     b->dbg_pairs, b->dbg_hsum,    b->dbg_hxor, b->dbg_cand,
                     b->dbg_acc,  b->dbg_cell};
     for (void* p : ptrs)
@@ -251,10 +254,23 @@ int upload_tables(plg_batch* b) {
         if (w.ntypes > 16) b->smem_matrix = false;
     }
     off[nw] = (int)b->n_total;
+    // Tiles of each world for every variant: a block never spans two worlds.
+    std::vector<int> toff((size_t)PLG_TILE_VARIANTS * (b->wcap + 1), 0);
+    for (int v = 0; v < PLG_TILE_VARIANTS; ++v) {
+        const int kt = tile_targets(b->dim, v);
+        int t = 0;
+        for (size_t k = 0; k < nw; ++k) {
+            toff[(size_t)v * (b->wcap + 1) + k] = t;
+            t += (int)((b->worlds[k].n + kt - 1) / kt);
+        }
+        toff[(size_t)v * (b->wcap + 1) + nw] = t;
+        b->tiles[v] = t;
+    }
     if (nb) BCK(b, cudaMemcpyAsync(b->bounds_d, bounds.data(), sizeof(float) * nb, cudaMemcpyHostToDevice, b->stream));
     if (nm) BCK(b, cudaMemcpyAsync(b->matrix_d, matrix.data(), sizeof(float) * nm, cudaMemcpyHostToDevice, b->stream));
     if (nw) BCK(b, cudaMemcpyAsync(b->worlds_d, fp.data(), sizeof(ForceParams) * nw, cudaMemcpyHostToDevice, b->stream));
     BCK(b, cudaMemcpyAsync(b->wp_off_d, off.data(), sizeof(int) * (nw + 1), cudaMemcpyHostToDevice, b->stream));
+    BCK(b, cudaMemcpyAsync(b->tile_off_d, toff.data(), sizeof(int) * toff.size(), cudaMemcpyHostToDevice, b->stream));
     // The host vectors die at return: wait for the copies.
     BCK(b, cudaStreamSynchronize(b->stream));
     return PLG_OK;
@@ -390,7 +406,8 @@ void enqueue_batch_step(plg_batch* b, const DebugOut* dbg, int32_t* cell_sorted)
     launch_scatter(st, n, b->cell, b->rank, b->cstart, b->perm, b->slot_cell);
     launch_gather<D>(st, n, b->perm, b->slot_cell, b->cstart, sbuf<D>(b->apt, b->avel, 0),
                      sbuf<D>(b->bpt, b->bvel, 0), cell_sorted);
-    launch_force_batch<D>(st, b->worlds_d, b->wp_off_d, (int)b->worlds.size(), n, b->smem_matrix,
+    launch_force_batch<D>(st, b->worlds_d, b->wp_off_d, b->tile_off_d + (size_t)b->variant * (b->wcap + 1),
+                          b->tiles[b->variant], (int)b->worlds.size(), n, b->smem_matrix,
                           sbuf<D>(b->bpt, b->bvel, 0), b->cstart, sbuf<D>(b->apt, b->avel, 0), b->cell, b->rank,
                           b->counts, b->defer, dbg, b->variant);
 }
@@ -498,6 +515,7 @@ int plg_batch_create(int32_t dim, int64_t particle_capacity, int32_t world_capac
     dm((void**)&b->status_d, 64);
     dm((void**)&b->worlds_d, sizeof(ForceParams) * wc);
     dm((void**)&b->wp_off_d, sizeof(int) * (wc + 1));
+    dm((void**)&b->tile_off_d, sizeof(int) * PLG_TILE_VARIANTS * (wc + 1));
     dm((void**)&b->move_new_d, sizeof(int) * (wc + 1));
     dm((void**)&b->move_old_d, sizeof(int) * wc);
     if (!rc && cudaMallocHost((void**)&b->status_h, 64) != cudaSuccess) rc = PLG_E_NO_MEMORY;

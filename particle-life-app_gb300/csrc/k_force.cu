@@ -67,10 +67,12 @@ struct ForceArgs {
     uint32_t* counts;
     uint32_t* defer_count;  // targets the tiled kernel deferred this step (statistics)
     DebugOut dbg;
-    // Batched worlds: per-world parameters and first sorted slots
-    // (wp_off[k] = worlds[k].p_off, nworlds + 1 entries).
+    // Batched worlds: per-world parameters, first sorted slots
+    // (wp_off[k] = worlds[k].p_off) and first tiles (tile_off[k] = the sum
+    // of ceil(n_j / kTargets) over j < k), nworlds + 1 entries each.
     const ForceParams* __restrict__ worlds;
     const int* __restrict__ wp_off;
+    const int* __restrict__ tile_off;
     int nworlds;
     int n_total;
 };
@@ -715,22 +717,18 @@ __device__ __noinline__ void fixup_target(const ForceArgs<D>& A, const ForcePara
     }
 }
 
-// Segment key of a target: its grid row, and in a batch its world in the
-// bits above kRowBits (worlds < 2^10, rows < 2^21).
-constexpr int kRowBits = 21;
-constexpr int kRowMask = (1 << kRowBits) - 1;
-
 // Main force kernel (nx >= 3): one thread per target; a block takes 256 (3D: 128)
-// consecutive targets and, per segment (targets of one grid row of one
-// world), stages the segment's stencil so that each target reads one
+// consecutive targets and, per segment (targets of one grid row), stages the segment's stencil so that each target reads one
 // contiguous run.  FP32 only and call-free: a target whose run meets a
 // candidate that needs the FP64 decision, or whose segment did not fit in
 // shared memory, is deferred to the block's closing pass (fixup_target),
 // which recomputes it completely.
 // BATCH: the sorted order holds many worlds one after another (their cells
-// are disjoint ranges of one global cell index); each target finds its
-// world's parameters in A.worlds, and segments never mix worlds, so every
-// target computes exactly what a single-world launch would.
+// are disjoint ranges of one global cell index).  Tiles are laid out per
+// world: block b works on tile b - tile_off[k] of the world k that owns it,
+// so a block never mixes worlds and every world is cut into exactly the
+// tiles a single-world launch uses: each world computes bit for bit what
+// plg_step computes for it, whatever else is in the batch.
 template <int D, bool DBG, bool SMEM_M, bool BATCH, int V>
 __global__ void __launch_bounds__(TileCfg<D, V>::kTargets, TileCfg<D, V>::kMinBlocks)
     k_force_tile(const __grid_constant__ ForceArgs<D> A) {
@@ -739,15 +737,20 @@ __global__ void __launch_bounds__(TileCfg<D, V>::kTargets, TileCfg<D, V>::kMinBl
     extern __shared__ __align__(16) unsigned char smraw[];
     TileSmem<D, V>& sm = *reinterpret_cast<TileSmem<D, V>*>(smraw);
     const int tid = threadIdx.x;
-    const int ntot = BATCH ? A.n_total : A.p.n;
-    const int s0 = blockIdx.x * kT;
-    const int nvalid = min(kT, ntot - s0);
+    int wk = 0, s0 = blockIdx.x * kT, nw = A.p.n;
+    if (BATCH) {
+        wk = world_of(A.tile_off, A.nworlds, blockIdx.x);
+        const int t = blockIdx.x - __ldg(A.tile_off + wk);
+        s0 = __ldg(A.wp_off + wk) + t * kT;
+        nw = __ldg(A.wp_off + wk + 1) - s0;  // targets of this world from s0 on
+    } else {
+        nw -= s0;
+    }
+    const int nvalid = min(kT, nw);
     const bool valid = tid < nvalid;
     const int s = s0 + tid;
-    int wk = 0;
-    if (BATCH && valid) wk = world_of(A.wp_off, A.nworlds, s);
     const ForceParams& P = BATCH ? A.worlds[wk] : A.p;
-    if (SMEM_M && !BATCH) {
+    if (SMEM_M) {
         const int nn = P.ntypes * P.ntypes;
         for (int k = tid; k < nn; k += kT) sm.mat[k] = P.matrix[k];
     }
@@ -760,7 +763,6 @@ __global__ void __launch_bounds__(TileCfg<D, V>::kTargets, TileCfg<D, V>::kMinBl
         const int cy = axis_cell(me.y, P.g);
         const int cz = D == 3 ? axis_cell(me.z, P.g) : 0;
         row = cy + cz * P.g.nx;
-        if (BATCH) row |= wk << kRowBits;
     }
     sm.rowid[tid] = row;
     sm.colid[tid] = cx;
@@ -788,17 +790,9 @@ __global__ void __launch_bounds__(TileCfg<D, V>::kTargets, TileCfg<D, V>::kMinBl
     bool defer = false;
     for (int g = 0; g < nseg; ++g) {
         const int ta = sm.seg[g], tb = sm.seg[g + 1];
-        const int key = sm.rowid[ta];
-        const int srow = BATCH ? key & kRowMask : key;
+        const int srow = sm.rowid[ta];
         const int cxa = sm.colid[ta], cxb = sm.colid[tb - 1];
-        const ForceParams& SP = BATCH ? A.worlds[key >> kRowBits] : A.p;  // the segment's world
-        if (SMEM_M && BATCH) {
-            // The previous segment's readers passed the barrier that ends its
-            // iteration; stage_segment's first barrier publishes the matrix.
-            const int nn = SP.ntypes * SP.ntypes;
-            for (int k = tid; k < nn; k += kT) sm.mat[k] = SP.matrix[k];
-        }
-        stage_segment<D, V>(A, SP, A.cstart + SP.cell_base, sm, srow, cxa, cxb);
+        stage_segment<D, V>(A, P, A.cstart + P.cell_base, sm, srow, cxa, cxb);
         if (tid >= ta && tid < tb) {
             if (sm.staged) {
                 const int nx = P.g.nx;
@@ -848,23 +842,14 @@ __global__ void __launch_bounds__(TileCfg<D, V>::kTargets, TileCfg<D, V>::kMinBl
     if (valid && defer) sm.rowid[dbefore + __popc(dm & ((1u << lane) - 1u))] = s;
     if (tid == 0) atomicAdd(A.defer_count, (uint32_t)nd);
     __syncthreads();
-    for (int d = warp; d < nd; d += kT / 32) {
-        const int t = sm.rowid[d];
-        if (BATCH) {
-            // The shared matrix belongs to the last segment's world: use the
-            // target's world's matrix in global memory.
-            const ForceParams& TP = A.worlds[world_of(A.wp_off, A.nworlds, t)];
-            fixup_target<D, DBG>(A, TP, A.cstart + TP.cell_base, TP.matrix, t, lane);
-        } else {
-            fixup_target<D, DBG>(A, A.p, A.cstart, M, t, lane);
-        }
-    }
+    for (int d = warp; d < nd; d += kT / 32) fixup_target<D, DBG>(A, P, A.cstart + P.cell_base, M, sm.rowid[d], lane);
 }
 
 template <int D, bool DBG, bool BATCH, int V>
-void launch_tile(cudaStream_t st, const ForceArgs<D>& A, bool smem_matrix) {
+void launch_tile(cudaStream_t st, const ForceArgs<D>& A, bool smem_matrix, int batch_tiles) {
     constexpr int kT = TileCfg<D, V>::kTargets;
-    const int grid = (A.n_total + kT - 1) / kT;
+    const int grid = BATCH ? batch_tiles : (A.n_total + kT - 1) / kT;
+    if (grid <= 0) return;
     const size_t sb = sizeof(TileSmem<D, V>);
     if (smem_matrix)
         k_force_tile<D, DBG, true, BATCH, V><<<grid, kT, sb, st>>>(A);
@@ -873,11 +858,11 @@ void launch_tile(cudaStream_t st, const ForceArgs<D>& A, bool smem_matrix) {
 }
 
 template <int D, bool DBG, bool BATCH>
-void launch_tile_variant(cudaStream_t st, const ForceArgs<D>& A, bool smem_matrix, int variant) {
+void launch_tile_variant(cudaStream_t st, const ForceArgs<D>& A, bool smem_matrix, int variant, int batch_tiles) {
     if (variant == 1)
-        launch_tile<D, DBG, BATCH, 1>(st, A, smem_matrix);
+        launch_tile<D, DBG, BATCH, 1>(st, A, smem_matrix, batch_tiles);
     else
-        launch_tile<D, DBG, BATCH, 0>(st, A, smem_matrix);
+        launch_tile<D, DBG, BATCH, 0>(st, A, smem_matrix, batch_tiles);
 }
 
 template <int D, bool DBG>
@@ -892,7 +877,7 @@ void launch_variant(cudaStream_t st, const ForceArgs<D>& A, bool general, int va
         else
             k_force_general<D, DBG, false><<<grid, kThreads, 0, st>>>(A);
     } else {
-        launch_tile_variant<D, DBG, false>(st, A, smem, variant);
+        launch_tile_variant<D, DBG, false>(st, A, smem, variant, 0);
     }
 }
 
@@ -913,6 +898,7 @@ ForceArgs<D> make_args(const ForceParams& p, StateBuf<D> b, const uint32_t* csta
     A.dbg = dbg ? *dbg : DebugOut{nullptr, nullptr, nullptr, nullptr, nullptr};
     A.worlds = nullptr;
     A.wp_off = nullptr;
+    A.tile_off = nullptr;
     A.nworlds = 1;
     A.n_total = p.n;
     return A;
@@ -933,28 +919,35 @@ void launch_force(cudaStream_t st, const ForceParams& p, bool general, StateBuf<
 }
 
 template <int D>
-void launch_force_batch(cudaStream_t st, const ForceParams* worlds, const int* wp_off, int nworlds, int n_total,
-                        bool smem_matrix, StateBuf<D> b, const uint32_t* cstart, StateBuf<D> a, uint32_t* cell,
-                        uint32_t* rank, uint32_t* counts, uint32_t* defer, const DebugOut* dbg, int variant) {
-    if (n_total <= 0 || nworlds <= 0) return;
+void launch_force_batch(cudaStream_t st, const ForceParams* worlds, const int* wp_off, const int* tile_off,
+                        int tiles, int nworlds, int n_total, bool smem_matrix, StateBuf<D> b, const uint32_t* cstart,
+                        StateBuf<D> a, uint32_t* cell, uint32_t* rank, uint32_t* counts, uint32_t* defer,
+                        const DebugOut* dbg, int variant) {
+    if (n_total <= 0 || nworlds <= 0 || tiles <= 0) return;
     ForceParams none{};
     ForceArgs<D> A = make_args<D>(none, b, cstart, a, cell, rank, counts, defer, dbg);
     A.worlds = worlds;
     A.wp_off = wp_off;
+    A.tile_off = tile_off;
     A.nworlds = nworlds;
     A.n_total = n_total;
     if (dbg)
-        launch_tile_variant<D, true, true>(st, A, smem_matrix, variant);
+        launch_tile_variant<D, true, true>(st, A, smem_matrix, variant, tiles);
     else
-        launch_tile_variant<D, false, true>(st, A, smem_matrix, variant);
+        launch_tile_variant<D, false, true>(st, A, smem_matrix, variant, tiles);
 }
 
-template void launch_force_batch<2>(cudaStream_t, const ForceParams*, const int*, int, int, bool, StateBuf<2>,
-                                    const uint32_t*, StateBuf<2>, uint32_t*, uint32_t*, uint32_t*, uint32_t*,
-                                    const DebugOut*, int);
-template void launch_force_batch<3>(cudaStream_t, const ForceParams*, const int*, int, int, bool, StateBuf<3>,
-                                    const uint32_t*, StateBuf<3>, uint32_t*, uint32_t*, uint32_t*, uint32_t*,
-                                    const DebugOut*, int);
+int tile_targets(int dim, int variant) {
+    if (dim == 2) return variant == 1 ? TileCfg<2, 1>::kTargets : TileCfg<2, 0>::kTargets;
+    return variant == 1 ? TileCfg<3, 1>::kTargets : TileCfg<3, 0>::kTargets;
+}
+
+template void launch_force_batch<2>(cudaStream_t, const ForceParams*, const int*, const int*, int, int, int, bool,
+                                    StateBuf<2>, const uint32_t*, StateBuf<2>, uint32_t*, uint32_t*, uint32_t*,
+                                    uint32_t*, const DebugOut*, int);
+template void launch_force_batch<3>(cudaStream_t, const ForceParams*, const int*, const int*, int, int, int, bool,
+                                    StateBuf<3>, const uint32_t*, StateBuf<3>, uint32_t*, uint32_t*, uint32_t*,
+                                    uint32_t*, const DebugOut*, int);
 
 template void launch_force<2>(cudaStream_t, const ForceParams&, bool, StateBuf<2>, const uint32_t*, StateBuf<2>,
                               uint32_t*, uint32_t*, uint32_t*, uint32_t*, const DebugOut*, int);

@@ -205,12 +205,18 @@ void launch_force(cudaStream_t st, const ForceParams& p, bool general, StateBuf<
 
 // Batched worlds: `worlds` (device, nworlds entries) holds each world's
 // parameters with its cell_base and p_off; `wp_off` (device, nworlds + 1)
-// the first sorted slot of each world and the total.  Every world has
-// nx >= 3.  smem_matrix: every world has at most 16 types.
+// the first sorted slot of each world and the total; `tile_off` (device,
+// nworlds + 1) the first tile of each world for this variant's tile size
+// (tile_targets), `tiles` the total.  Every world has nx >= 3.
+// smem_matrix: every world has at most 16 types.
 template <int D>
-void launch_force_batch(cudaStream_t st, const ForceParams* worlds, const int* wp_off, int nworlds, int n_total,
-                        bool smem_matrix, StateBuf<D> b, const uint32_t* cstart, StateBuf<D> a, uint32_t* cell,
-                        uint32_t* rank, uint32_t* counts, uint32_t* defer, const DebugOut* dbg, int variant = 0);
+void launch_force_batch(cudaStream_t st, const ForceParams* worlds, const int* wp_off, const int* tile_off,
+                        int tiles, int nworlds, int n_total, bool smem_matrix, StateBuf<D> b, const uint32_t* cstart,
+                        StateBuf<D> a, uint32_t* cell, uint32_t* rank, uint32_t* counts, uint32_t* defer,
+                        const DebugOut* dbg, int variant = 0);
+
+// Targets per block of the force kernel's tile variant.
+int tile_targets(int dim, int variant);
 
 // Opts the tiled force kernel in to its dynamic shared memory (> 48 KB) on
 // the current device; called once per context.
