@@ -218,6 +218,14 @@ typedef struct plg_world_desc {
     const int32_t* type;     /* int32[n], 0 <= type < ntypes */
 } plg_world_desc;
 
+/* The checks plg_batch_update applies to one world description, without a
+ * device: PLG_OK, PLG_E_INVALID_ARG, PLG_E_UNSUPPORTED or PLG_E_CAPACITY.
+ * Host only. */
+int plg_world_check(int32_t dim, const plg_world_desc* world);
+/* Device bytes a world occupies in a batch (particles, cells, tables).
+ * Host only; -1 for a bad argument. */
+int64_t plg_world_device_bytes(int32_t dim, const plg_world_desc* world);
+
 /* Capacities: particles, worlds (<= 1024) and cells over all worlds. */
 int plg_batch_create(int32_t dim, int64_t particle_capacity, int32_t world_capacity,
                      int64_t cell_capacity, plg_batch** out);
@@ -265,6 +273,55 @@ int plg_batch_autotune(plg_batch* batch, int32_t steps, int32_t* chosen, double*
 int plg_batch_debug_step(plg_batch* batch, int32_t* cell, int32_t* pairs,
                          uint64_t* hash_sum, uint64_t* hash_xor, float* acc,
                          int64_t* candidates);
+
+/* ---- serving ----------------------------------------------------------- */
+
+/* A request loop over batched worlds (no counterpart in the reference):
+ * requests (a world and a step count) are submitted from any thread; a
+ * native scheduler thread admits them first-in-first-out as the device
+ * memory budget and the batch capacities allow, keeps their worlds resident,
+ * packs every active world into one batch per dimension (the 2D and 3D
+ * batches run concurrently on their own streams), advances them in chunks
+ * of at most max_chunk_steps steps (never past a world's own count) and
+ * hands back each final state.  Requests that arrive while others run join
+ * at the next chunk boundary.  Each result is bit for bit the world run
+ * alone. */
+typedef struct plg_server plg_server;
+
+typedef struct plg_server_config {
+    int64_t memory_budget_bytes;   /* admission limit: sum of resident worlds' plg_world_device_bytes */
+    int64_t particle_capacity[2];  /* batch capacities [2D, 3D] (allocated at create) */
+    int64_t cell_capacity[2];
+    int32_t max_worlds_per_batch;  /* <= 1024 */
+    int32_t max_chunk_steps;       /* steps between admissions */
+    int32_t tile_variant;          /* force kernel tile variant, fixed for the server's life */
+} plg_server_config;
+
+#define PLG_REQ_QUEUED 0
+#define PLG_REQ_RUNNING 1
+#define PLG_REQ_DONE 2
+
+typedef struct plg_server_stats_t {
+    int64_t submitted, completed, queued, running;
+    int64_t resident_bytes, peak_resident_bytes;
+    double particle_steps;   /* advanced so far, all worlds */
+    double busy_s, wall_s;   /* time the scheduler spent in chunks / since create */
+    double latency_p50_ms, latency_p99_ms, latency_mean_ms;  /* submit -> result on host */
+} plg_server_stats_t;
+
+int plg_server_create(const plg_server_config* cfg, plg_server** out);
+/* Copies the world; PLG_E_CAPACITY for a request that could never fit. */
+int plg_server_submit(plg_server* server, int32_t dim, const plg_world_desc* world, int32_t steps,
+                      int64_t* request_id);
+/* Waits for a request (timeout_s <= 0: no limit); *state = PLG_REQ_*. */
+int plg_server_wait(plg_server* server, int64_t request_id, double timeout_s, int32_t* state);
+/* Copies a finished request's final state (cell-sorted order, like
+ * plg_download) and releases it; any pointer may be NULL. */
+int plg_server_result(plg_server* server, int64_t request_id, double* pos, double* vel, int32_t* type,
+                      int32_t* pid, int64_t* n, double* latency_ms);
+int plg_server_stats(plg_server* server, plg_server_stats_t* out);
+const char* plg_server_last_error(plg_server* server);
+int plg_server_destroy(plg_server* server);
 
 /* ---- cell sort without allocation ------------------------------------- */
 

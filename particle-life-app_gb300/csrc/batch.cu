@@ -198,29 +198,36 @@ int find_world(const plg_batch* b, int32_t id) {
 
 // Host-side checks of one world description (the device path has no CPU
 // fallback, so anything it cannot run is rejected here).
-int check_desc(plg_batch* b, const plg_world_desc& d) {
-    int rc = plg_validate_settings(b->dim, &d.settings);
-    if (rc) return berr(b, rc, "world settings rejected by plg_validate_settings");
-    if (grid_n(d.settings.rmax) < 3)
-        return berr(b, PLG_E_UNSUPPORTED, "batched worlds need rmax <= 1/3 (>= 3 cells per axis)");
-    if (d.ntypes < 1 || d.ntypes > kMaxTypes) return berr(b, PLG_E_INVALID_ARG, "matrix size must be 1..1024");
-    if (!d.matrix) return berr(b, PLG_E_INVALID_ARG, "matrix must not be NULL");
+int check_world(int dim, const plg_world_desc& d, std::string* msg) {
+    auto fail = [&](int code, const char* m) {
+        if (msg) *msg = m;
+        return code;
+    };
+    int rc = plg_validate_settings(dim, &d.settings);
+    if (rc) return fail(rc, "world settings rejected by plg_validate_settings");
+    if (grid_n(d.settings.rmax) < 3) return fail(PLG_E_UNSUPPORTED, "batched worlds need rmax <= 1/3 (>= 3 cells per axis)");
+    if (d.ntypes < 1 || d.ntypes > kMaxTypes) return fail(PLG_E_INVALID_ARG, "matrix size must be 1..1024");
+    if (!d.matrix) return fail(PLG_E_INVALID_ARG, "matrix must not be NULL");
     for (int64_t k = 0; k < (int64_t)d.ntypes * d.ntypes; ++k)
-        if (!std::isfinite(d.matrix[k])) return berr(b, PLG_E_INVALID_ARG, "matrix entries must be finite");
-    if (d.n < 0) return berr(b, PLG_E_INVALID_ARG, "negative particle count");
-    if (d.n > 0 && (!d.pos || !d.type)) return berr(b, PLG_E_INVALID_ARG, "pos and type must not be NULL");
+        if (!std::isfinite(d.matrix[k])) return fail(PLG_E_INVALID_ARG, "matrix entries must be finite");
+    if (d.n < 0) return fail(PLG_E_INVALID_ARG, "negative particle count");
+    if (d.n > kMaxParticles) return fail(PLG_E_CAPACITY, "too many particles");
+    if (d.n > 0 && (!d.pos || !d.type)) return fail(PLG_E_INVALID_ARG, "pos and type must not be NULL");
     for (int64_t i = 0; i < d.n; ++i) {
-        for (int k = 0; k < b->dim; ++k) {
+        for (int k = 0; k < dim; ++k) {
             const double x = d.pos[3 * i + k];
-            if (!(x >= 0.0 && x <= 1.0))
-                return berr(b, PLG_E_INVALID_ARG, "positions must lie in [0,1] (ensurePosition first)");
-            if (d.vel && !std::isfinite(d.vel[3 * i + k]))
-                return berr(b, PLG_E_INVALID_ARG, "velocities must be finite");
+            if (!(x >= 0.0 && x <= 1.0)) return fail(PLG_E_INVALID_ARG, "positions must lie in [0,1] (ensurePosition first)");
+            if (d.vel && !std::isfinite(d.vel[3 * i + k])) return fail(PLG_E_INVALID_ARG, "velocities must be finite");
         }
-        if (d.type[i] < 0 || d.type[i] >= d.ntypes)
-            return berr(b, PLG_E_INVALID_ARG, "types must lie in [0, matrix size)");
+        if (d.type[i] < 0 || d.type[i] >= d.ntypes) return fail(PLG_E_INVALID_ARG, "types must lie in [0, matrix size)");
     }
     return PLG_OK;
+}
+
+int check_desc(plg_batch* b, const plg_world_desc& d) {
+    std::string msg;
+    const int rc = check_world(b->dim, d, &msg);
+    return rc ? berr(b, rc, msg) : PLG_OK;
 }
 
 // Writes the device world tables for the current b->worlds layout.
@@ -469,6 +476,19 @@ int wait_batch(plg_batch* b, double timeout_s) {
 }  // namespace
 
 extern "C" {
+
+int plg_world_check(int32_t dim, const plg_world_desc* d) {
+    if (!d || (dim != 2 && dim != 3)) return PLG_E_INVALID_ARG;
+    return check_world(dim, *d, nullptr);
+}
+
+int64_t plg_world_device_bytes(int32_t dim, const plg_world_desc* d) {
+    if (!d || (dim != 2 && dim != 3) || !(d->settings.rmax > 0 && d->settings.rmax <= 1)) return -1;
+    const int64_t nx = grid_n(d->settings.rmax);
+    const int64_t cells = nx * nx * (dim == 3 ? nx : 1);
+    const int64_t per_particle = dim == 2 ? 2 * (16 + 8) + 4 * 4 : 2 * (16 + 16) + 4 * 4;
+    return d->n * per_particle + cells * 8 + (nx + 1) * 4 + (int64_t)d->ntypes * d->ntypes * 4;
+}
 
 int plg_batch_create(int32_t dim, int64_t particle_capacity, int32_t world_capacity, int64_t cell_capacity,
                      plg_batch** out) {

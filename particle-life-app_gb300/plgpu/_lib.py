@@ -56,6 +56,39 @@ class plg_world_desc(C.Structure):
     ]
 
 
+class plg_server_config(C.Structure):
+    _fields_ = [
+        ("memory_budget_bytes", C.c_int64),
+        ("particle_capacity", C.c_int64 * 2),
+        ("cell_capacity", C.c_int64 * 2),
+        ("max_worlds_per_batch", C.c_int32),
+        ("max_chunk_steps", C.c_int32),
+        ("tile_variant", C.c_int32),
+    ]
+
+
+class plg_server_stats_t(C.Structure):
+    _fields_ = [
+        ("submitted", C.c_int64),
+        ("completed", C.c_int64),
+        ("queued", C.c_int64),
+        ("running", C.c_int64),
+        ("resident_bytes", C.c_int64),
+        ("peak_resident_bytes", C.c_int64),
+        ("particle_steps", C.c_double),
+        ("busy_s", C.c_double),
+        ("wall_s", C.c_double),
+        ("latency_p50_ms", C.c_double),
+        ("latency_p99_ms", C.c_double),
+        ("latency_mean_ms", C.c_double),
+    ]
+
+
+PLG_REQ_QUEUED = 0
+PLG_REQ_RUNNING = 1
+PLG_REQ_DONE = 2
+
+
 class PlgError(RuntimeError):
     """A plg_* call returned a non-zero status."""
 
@@ -116,6 +149,15 @@ SIGNATURES = {
     "plg_batch_set_tile": (C.c_int, [_P, C.c_int32]),
     "plg_batch_get_tile": (C.c_int, [_P, _I32P]),
     "plg_batch_autotune": (C.c_int, [_P, C.c_int32, _I32P, _DP]),
+    "plg_world_check": (C.c_int, [C.c_int32, C.POINTER(plg_world_desc)]),
+    "plg_world_device_bytes": (C.c_int64, [C.c_int32, C.POINTER(plg_world_desc)]),
+    "plg_server_create": (C.c_int, [C.POINTER(plg_server_config), C.POINTER(_P)]),
+    "plg_server_submit": (C.c_int, [_P, C.c_int32, C.POINTER(plg_world_desc), C.c_int32, _I64P]),
+    "plg_server_wait": (C.c_int, [_P, C.c_int64, C.c_double, _I32P]),
+    "plg_server_result": (C.c_int, [_P, C.c_int64, _DP, _DP, _I32P, _I32P, _I64P, _DP]),
+    "plg_server_stats": (C.c_int, [_P, C.POINTER(plg_server_stats_t)]),
+    "plg_server_last_error": (C.c_char_p, [_P]),
+    "plg_server_destroy": (C.c_int, [_P]),
 }
 
 _lib = None

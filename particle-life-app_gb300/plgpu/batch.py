@@ -30,6 +30,25 @@ class WorldDesc:
     vel: Optional[np.ndarray] = None
 
 
+def world_struct(w: WorldDesc, keep: list) -> "_lib.plg_world_desc":
+    """The C description of a world; `keep` receives the arrays it points to."""
+    pos = np.ascontiguousarray(w.pos, dtype=np.float64).reshape(-1, 3)
+    types = np.ascontiguousarray(w.types, dtype=np.int32)
+    m = np.ascontiguousarray(w.matrix, dtype=np.float64)
+    vel = None if w.vel is None else np.ascontiguousarray(w.vel, dtype=np.float64).reshape(-1, 3)
+    keep += [pos, types, m, vel]
+    d = _lib.plg_world_desc()
+    d.settings = _lib.plg_settings(w.rmax, w.friction, w.force, w.dt, w.beta, 1 if w.wrap else 0,
+                                   _lib.PLG_ACCEL_PARTICLE_LIFE)
+    d.ntypes = m.shape[0]
+    d.matrix = _lib.ptr(m, _lib.C.c_double)
+    d.n = pos.shape[0]
+    d.pos = _lib.ptr(pos, _lib.C.c_double)
+    d.vel = _lib.ptr(vel, _lib.C.c_double) if vel is not None else None
+    d.type = _lib.ptr(types, _lib.C.c_int32)
+    return d
+
+
 def _check(status: int, b, what: str) -> None:
     if status != _lib.PLG_OK:
         lib = _lib.load()
@@ -59,23 +78,10 @@ class GpuBatch:
 
     def update(self, remove: Sequence[int] = (), add: Sequence[WorldDesc] = ()) -> list[int]:
         """Removes worlds by id and adds new ones; returns the new ids."""
-        keep = []
+        keep: list = []
         descs = (_lib.plg_world_desc * max(len(add), 1))()
         for k, w in enumerate(add):
-            pos = np.ascontiguousarray(w.pos, dtype=np.float64).reshape(-1, 3)
-            types = np.ascontiguousarray(w.types, dtype=np.int32)
-            m = np.ascontiguousarray(w.matrix, dtype=np.float64)
-            vel = None if w.vel is None else np.ascontiguousarray(w.vel, dtype=np.float64).reshape(-1, 3)
-            keep += [pos, types, m, vel]
-            d = descs[k]
-            d.settings = _lib.plg_settings(w.rmax, w.friction, w.force, w.dt, w.beta, 1 if w.wrap else 0,
-                                           _lib.PLG_ACCEL_PARTICLE_LIFE)
-            d.ntypes = m.shape[0]
-            d.matrix = _lib.ptr(m, _lib.C.c_double)
-            d.n = pos.shape[0]
-            d.pos = _lib.ptr(pos, _lib.C.c_double)
-            d.vel = _lib.ptr(vel, _lib.C.c_double) if vel is not None else None
-            d.type = _lib.ptr(types, _lib.C.c_int32)
+            descs[k] = world_struct(w, keep)
         rem = np.ascontiguousarray(list(remove), dtype=np.int32)
         ids = np.zeros(max(len(add), 1), np.int32)
         _check(self.lib.plg_batch_update(self.b, len(rem), _lib.ptr(rem, _lib.C.c_int32) if len(rem) else None,

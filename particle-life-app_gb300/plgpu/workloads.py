@@ -46,3 +46,23 @@ def batched_worlds(count: int = 512, seed: int = 7, n_lo: int = 1_000, n_hi: int
 
 def cells_of(w: WorldDesc, dim: int) -> int:
     return int(math.floor(1.0 / w.rmax)) ** dim
+
+
+def serving_request(rng: np.random.Generator, n_lo: int = 1_000, n_hi: int = 2_000_000, steps_lo: int = 100,
+                    steps_hi: int = 5_000) -> tuple[int, WorldDesc, int]:
+    """One request of the served configuration: 2D or 3D (50/50), N
+    log-uniform in [n_lo, n_hi], types uniform in 3..16, matrix uniform in
+    [-1,1], rmax giving k uniform in [10, 50] expected neighbours
+    (2D: k = pi n rmax^2, 3D: k = 4/3 pi n rmax^3), friction half-life
+    0.043 s, dt 0.02, step count uniform in [steps_lo, steps_hi]."""
+    dim = 2 if rng.random() < 0.5 else 3
+    n = int(round(math.exp(rng.uniform(math.log(n_lo), math.log(n_hi)))))
+    ntypes = int(rng.integers(3, 17))
+    k = float(rng.uniform(10, 50))
+    if dim == 2:
+        rmax = math.sqrt(k / (math.pi * n))
+    else:
+        rmax = (3 * k / (4 * math.pi * n)) ** (1 / 3)
+    rmax = min(rmax, 0.3)
+    steps = int(rng.integers(steps_lo, steps_hi + 1))
+    return dim, random_world(rng, dim, n, ntypes, rmax, friction_of_half_life(0.043), 0.02), steps
