@@ -58,12 +58,15 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=1_000_000)
     ap.add_argument("--e2e-steps", type=int, default=30)
-    ap.add_argument("--cpu-sample-s", type=float, default=10.0)
+    ap.add_argument("--cpu-sample-s", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-flush", action="store_true", help="keep L2 warm between steps (not a headline number)")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-worlds measurement")
     ap.add_argument("--batched-worlds", type=int, default=512)
     ap.add_argument("--batched-steps", type=int, default=20)
+    ap.add_argument("--no-serving", action="store_true", help="skip the serving measurement")
+    ap.add_argument("--serve-seconds", type=float, default=10.0)
+    ap.add_argument("--serve-rate", type=float, default=200.0)
     return ap.parse_args()
 
 
@@ -134,8 +137,9 @@ def cpu_oracle_rate(n, threads, budget_s, steps_cap=None):
     w = orc.World(2, pos, vel, types, np.arange(n, dtype=np.int32), m,
                   orc.settings(SETTINGS["rmax"], SETTINGS["friction"], SETTINGS["force"], SETTINGS["dt"],
                                SETTINGS["beta"], SETTINGS["wrap"]))
-    t1 = w.run(1, threads)  # warm-up and estimate
-    steps = max(1, int(budget_s / max(t1, 1e-6)))
+    w.run(1, threads)  # warm-up
+    t2 = w.run(2, threads) / 2  # estimate
+    steps = max(1, int(budget_s / max(t2, 1e-6)))
     if steps_cap:
         steps = min(steps, steps_cap)
     t = w.run(steps, threads)
@@ -195,6 +199,50 @@ def run_batched(args) -> dict:
             "autotune": {"chosen_tile_variant": variant, "ms_per_step_by_variant": tune_ms},
             "config": "512 2D periodic worlds, N log-uniform [1e3, 2e5], types 3..12, rmax U[0.005, 0.03] "
                       "(unit box), friction t1/2 U[0.02, 0.1] s, dt 0.02; seeded Philox"}
+
+
+def run_serving(args) -> dict:
+    """The served configuration, bounded: Poisson arrivals at the configured
+    rate (200/s) for --serve-seconds, 50/50 2D/3D, types 3..16, k in [10, 50]
+    neighbours, 150 GB admission budget; N and steps are scaled down
+    (N log-uniform [1e3, 2e5] instead of [1e3, 2e6], steps U[100, 1000]
+    instead of [100, 5000]) so that the offered load stays near the device's
+    capacity and the run drains in about a minute."""
+    from plgpu import workloads
+    from plgpu.serve import Server
+
+    rng = np.random.Generator(np.random.Philox(2025))
+    count = int(args.serve_rate * args.serve_seconds)
+    reqs = [workloads.serving_request(rng, n_lo=1_000, n_hi=200_000, steps_lo=100, steps_hi=1_000)
+            for _ in range(count)]
+    gaps = rng.exponential(1.0 / args.serve_rate, count)
+    offered = sum(w.pos.shape[0] * st for _, w, st in reqs) / args.serve_seconds
+    srv = Server(memory_budget_bytes=150 << 30, particle_capacity=(40_000_000, 40_000_000),
+                 cell_capacity=(60_000_000, 60_000_000), max_worlds_per_batch=1024, max_chunk_steps=16)
+    t0 = time.perf_counter()
+    due = t0
+    ids = []
+    for (dim, w, st), gap in zip(reqs, gaps):
+        due += gap
+        delay = due - time.perf_counter()
+        if delay > 0:
+            time.sleep(delay)
+        ids.append(srv.submit(dim, w, st))
+    for rid in ids:
+        srv.wait(rid, 600.0)
+    wall = time.perf_counter() - t0
+    st = srv.stats()
+    for rid in ids:
+        srv.result(rid)
+    srv.close()
+    return {"metric": "served requests: completion latency and aggregate particle-steps/s",
+            "requests": count, "completed": st["completed"], "latency_p50_ms": st["latency_p50_ms"],
+            "latency_p99_ms": st["latency_p99_ms"], "latency_mean_ms": st["latency_mean_ms"],
+            "value": st["particle_steps"] / wall, "unit": UNIT, "offered_particle_steps_per_s": offered,
+            "wall_s": wall, "peak_resident_bytes": st["peak_resident_bytes"],
+            "config": f"Poisson arrivals {args.serve_rate:g}/s for {args.serve_seconds:g} s, 2D/3D 50/50, "
+                      "N log-uniform [1e3, 2e5], types 3..16, k U[10, 50], steps U[100, 1000], budget 150 GB, "
+                      "chunks of <= 16 steps; seeded Philox"}
 
 
 def run_reference(args):
@@ -378,6 +426,9 @@ def run_ours(args):
     batched = None
     if rank == 0 and not args.no_batched:
         batched = run_batched(args)
+    serving = None
+    if rank == 0 and not args.no_serving:
+        serving = run_serving(args)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -411,6 +462,7 @@ def run_ours(args):
             "interactions_per_particle": inter,
             "cpu_baseline": cpu,
             "batched": batched,
+            "serving": serving,
             "clocks": clk,
         }
         print(json.dumps(line))

@@ -244,6 +244,12 @@ int plg_batch_step(plg_batch* batch, int32_t nsteps);
 int plg_batch_step_async(plg_batch* batch, int32_t nsteps);
 int plg_batch_sync(plg_batch* batch, double timeout_s);
 
+/* Step budget of one world: after `steps` more batch steps the world
+ * freezes (keeps its state while the others advance).  steps < 0: no limit
+ * (the default).  plg_batch_steps_left reports -1 for no limit. */
+int plg_batch_set_steps(plg_batch* batch, int32_t id, int32_t steps);
+int plg_batch_steps_left(plg_batch* batch, int32_t id, int32_t* steps);
+
 /* One world's state in its cell-sorted order, like plg_download. */
 int plg_batch_download(plg_batch* batch, int32_t id, double* pos, double* vel,
                        int32_t* type, int32_t* pid);

@@ -42,6 +42,7 @@ struct WorldRec {
     std::vector<float> bounds;  // nx + 1
     std::vector<float> matrix;  // ntypes^2
     int64_t p_off = 0, c_off = 0, m_off = 0, b_off = 0;
+    int32_t steps_left = INT32_MAX;  // steps before the world freezes (INT32_MAX: no limit)
 };
 
 }  // namespace
@@ -71,6 +72,7 @@ struct plg_batch {
     ForceParams* worlds_d = nullptr;  // wcap
     int* wp_off_d = nullptr;          // wcap + 1
     int* tile_off_d = nullptr;        // PLG_TILE_VARIANTS x (wcap + 1): first tile of each world
+    int* steps_left_d = nullptr;      // wcap: device countdown, a world at 0 is frozen
     int tiles[PLG_TILE_VARIANTS] = {};
     int* move_new_d = nullptr;        // wcap + 1
     int* move_old_d = nullptr;        // wcap
@@ -181,7 +183,7 @@ void free_batch(plg_batch* b) {
     void* ptrs[] = {b->apt,      b->bpt,       b->avel,      b->bvel,        b->cell,     b->rank,
                     b->perm,     b->slot_cell, b->counts,    b->cstart,      b->scan_state, b->defer,
                     b->status_d, b->worlds_d,  b->wp_off_d,  b->move_new_d,  b->move_old_d, b->bounds_d,
-                    b->tile_off_d,
+                    b->tile_off_d, b->steps_left_d,
                     b->matrix_d, b->stage,     b->dbg_pairs, b->dbg_hsum,    b->dbg_hxor, b->dbg_cand,
                     b->dbg_acc,  b->dbg_cell};
     for (void* p : ptrs)
@@ -278,6 +280,9 @@ int upload_tables(plg_batch* b) {
     if (nw) BCK(b, cudaMemcpyAsync(b->worlds_d, fp.data(), sizeof(ForceParams) * nw, cudaMemcpyHostToDevice, b->stream));
     BCK(b, cudaMemcpyAsync(b->wp_off_d, off.data(), sizeof(int) * (nw + 1), cudaMemcpyHostToDevice, b->stream));
     BCK(b, cudaMemcpyAsync(b->tile_off_d, toff.data(), sizeof(int) * toff.size(), cudaMemcpyHostToDevice, b->stream));
+    std::vector<int> left(std::max<size_t>(nw, 1));
+    for (size_t k = 0; k < nw; ++k) left[k] = b->worlds[k].steps_left;
+    if (nw) BCK(b, cudaMemcpyAsync(b->steps_left_d, left.data(), sizeof(int) * nw, cudaMemcpyHostToDevice, b->stream));
     // The host vectors die at return: wait for the copies.
     BCK(b, cudaStreamSynchronize(b->stream));
     return PLG_OK;
@@ -414,9 +419,10 @@ void enqueue_batch_step(plg_batch* b, const DebugOut* dbg, int32_t* cell_sorted)
     launch_gather<D>(st, n, b->perm, b->slot_cell, b->cstart, sbuf<D>(b->apt, b->avel, 0),
                      sbuf<D>(b->bpt, b->bvel, 0), cell_sorted);
     launch_force_batch<D>(st, b->worlds_d, b->wp_off_d, b->tile_off_d + (size_t)b->variant * (b->wcap + 1),
-                          b->tiles[b->variant], (int)b->worlds.size(), n, b->smem_matrix,
+                          b->steps_left_d, b->tiles[b->variant], (int)b->worlds.size(), n, b->smem_matrix,
                           sbuf<D>(b->bpt, b->bvel, 0), b->cstart, sbuf<D>(b->apt, b->avel, 0), b->cell, b->rank,
                           b->counts, b->defer, dbg, b->variant);
+    launch_batch_tick(st, b->steps_left_d, (int)b->worlds.size());
 }
 
 int enqueue_step(plg_batch* b) {
@@ -536,6 +542,7 @@ int plg_batch_create(int32_t dim, int64_t particle_capacity, int32_t world_capac
     dm((void**)&b->worlds_d, sizeof(ForceParams) * wc);
     dm((void**)&b->wp_off_d, sizeof(int) * (wc + 1));
     dm((void**)&b->tile_off_d, sizeof(int) * PLG_TILE_VARIANTS * (wc + 1));
+    dm((void**)&b->steps_left_d, sizeof(int) * wc);
     dm((void**)&b->move_new_d, sizeof(int) * (wc + 1));
     dm((void**)&b->move_old_d, sizeof(int) * wc);
     if (!rc && cudaMallocHost((void**)&b->status_h, 64) != cudaSuccess) rc = PLG_E_NO_MEMORY;
@@ -590,6 +597,29 @@ int plg_batch_step_async(plg_batch* b, int32_t nsteps) {
         const int rc = enqueue_step(b);
         if (rc) return rc;
     }
+    for (WorldRec& w : b->worlds)  // mirror of the device countdown
+        if (w.steps_left != INT32_MAX) w.steps_left = std::max<int32_t>(0, w.steps_left - nsteps);
+    return PLG_OK;
+}
+
+int plg_batch_set_steps(plg_batch* b, int32_t id, int32_t steps) {
+    if (!b) return PLG_E_INVALID_ARG;
+    const int k = find_world(b, id);
+    if (k < 0) return berr(b, PLG_E_INVALID_ARG, "unknown world id " + std::to_string(id));
+    if (steps < 0) steps = INT32_MAX;
+    BatchDeviceGuard g(b->device);
+    b->worlds[(size_t)k].steps_left = steps;
+    const int v = steps;
+    BCK(b, cudaMemcpyAsync(b->steps_left_d + k, &v, sizeof(int), cudaMemcpyHostToDevice, b->stream));
+    BCK(b, cudaStreamSynchronize(b->stream));
+    return PLG_OK;
+}
+
+int plg_batch_steps_left(plg_batch* b, int32_t id, int32_t* steps) {
+    if (!b || !steps) return PLG_E_INVALID_ARG;
+    const int k = find_world(b, id);
+    if (k < 0) return berr(b, PLG_E_INVALID_ARG, "unknown world id " + std::to_string(id));
+    *steps = b->worlds[(size_t)k].steps_left == INT32_MAX ? -1 : b->worlds[(size_t)k].steps_left;
     return PLG_OK;
 }
 

@@ -155,6 +155,11 @@ __global__ void __launch_bounds__(kThreads) k_batch_rebin(int n, StateBuf<D> a, 
     }
 }
 
+__global__ void k_batch_tick(int* steps_left, int nworlds) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < nworlds && steps_left[k] > 0) steps_left[k] -= 1;
+}
+
 // Re-binning of the current state (after an rmax change).
 template <int D>
 __global__ void __launch_bounds__(kThreads) k_rebin(int n, StateBuf<D> a, uint32_t* __restrict__ cell,
@@ -406,6 +411,11 @@ void launch_batch_rebin(cudaStream_t st, int n, StateBuf<D> a, const ForceParams
                         uint32_t* cell, uint32_t* rank, uint32_t* counts) {
     if (n <= 0 || nw <= 0) return;
     k_batch_rebin<D><<<blocks_for(n, kThreads), kThreads, 0, st>>>(n, a, worlds, wp_off, nw, cell, rank, counts);
+}
+
+void launch_batch_tick(cudaStream_t st, int* steps_left, int nworlds) {
+    if (nworlds <= 0 || !steps_left) return;
+    k_batch_tick<<<blocks_for(nworlds, kThreads), kThreads, 0, st>>>(steps_left, nworlds);
 }
 
 template void launch_batch_move<2>(cudaStream_t, int, const int*, const int*, int, StateBuf<2>, StateBuf<2>);

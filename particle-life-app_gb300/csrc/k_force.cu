@@ -73,6 +73,7 @@ struct ForceArgs {
     const ForceParams* __restrict__ worlds;
     const int* __restrict__ wp_off;
     const int* __restrict__ tile_off;
+    const int* __restrict__ steps_left;  // per world; <= 0: frozen this step (may be null)
     int nworlds;
     int n_total;
 };
@@ -750,6 +751,18 @@ __global__ void __launch_bounds__(TileCfg<D, V>::kTargets, TileCfg<D, V>::kMinBl
     const bool valid = tid < nvalid;
     const int s = s0 + tid;
     const ForceParams& P = BATCH ? A.worlds[wk] : A.p;
+    if (BATCH && A.steps_left && __ldg(A.steps_left + wk) <= 0) {
+        // A world that has used up its steps is left exactly as its last
+        // step left it: A (its state, in that step's order) is not touched,
+        // and the cells that step computed for it are counted again for the
+        // next sort (the scan consumed the counts).  A world's slots are the
+        // same range in A and B, so this tile's slots are its A slots.
+        uint32_t c = 0;
+        if (valid) c = A.cell[s];
+        const unsigned m = __ballot_sync(kFull, valid);
+        if (valid) A.rank[s] = bin_count(A.counts, c, m);
+        return;
+    }
     if (SMEM_M) {
         const int nn = P.ntypes * P.ntypes;
         for (int k = tid; k < nn; k += kT) sm.mat[k] = P.matrix[k];
@@ -899,6 +912,7 @@ ForceArgs<D> make_args(const ForceParams& p, StateBuf<D> b, const uint32_t* csta
     A.worlds = nullptr;
     A.wp_off = nullptr;
     A.tile_off = nullptr;
+    A.steps_left = nullptr;
     A.nworlds = 1;
     A.n_total = p.n;
     return A;
@@ -920,15 +934,16 @@ void launch_force(cudaStream_t st, const ForceParams& p, bool general, StateBuf<
 
 template <int D>
 void launch_force_batch(cudaStream_t st, const ForceParams* worlds, const int* wp_off, const int* tile_off,
-                        int tiles, int nworlds, int n_total, bool smem_matrix, StateBuf<D> b, const uint32_t* cstart,
-                        StateBuf<D> a, uint32_t* cell, uint32_t* rank, uint32_t* counts, uint32_t* defer,
-                        const DebugOut* dbg, int variant) {
+                        const int* steps_left, int tiles, int nworlds, int n_total, bool smem_matrix, StateBuf<D> b,
+                        const uint32_t* cstart, StateBuf<D> a, uint32_t* cell, uint32_t* rank, uint32_t* counts,
+                        uint32_t* defer, const DebugOut* dbg, int variant) {
     if (n_total <= 0 || nworlds <= 0 || tiles <= 0) return;
     ForceParams none{};
     ForceArgs<D> A = make_args<D>(none, b, cstart, a, cell, rank, counts, defer, dbg);
     A.worlds = worlds;
     A.wp_off = wp_off;
     A.tile_off = tile_off;
+    A.steps_left = steps_left;
     A.nworlds = nworlds;
     A.n_total = n_total;
     if (dbg)
@@ -942,12 +957,12 @@ int tile_targets(int dim, int variant) {
     return variant == 1 ? TileCfg<3, 1>::kTargets : TileCfg<3, 0>::kTargets;
 }
 
-template void launch_force_batch<2>(cudaStream_t, const ForceParams*, const int*, const int*, int, int, int, bool,
-                                    StateBuf<2>, const uint32_t*, StateBuf<2>, uint32_t*, uint32_t*, uint32_t*,
-                                    uint32_t*, const DebugOut*, int);
-template void launch_force_batch<3>(cudaStream_t, const ForceParams*, const int*, const int*, int, int, int, bool,
-                                    StateBuf<3>, const uint32_t*, StateBuf<3>, uint32_t*, uint32_t*, uint32_t*,
-                                    uint32_t*, const DebugOut*, int);
+template void launch_force_batch<2>(cudaStream_t, const ForceParams*, const int*, const int*, const int*, int, int,
+                                    int, bool, StateBuf<2>, const uint32_t*, StateBuf<2>, uint32_t*, uint32_t*,
+                                    uint32_t*, uint32_t*, const DebugOut*, int);
+template void launch_force_batch<3>(cudaStream_t, const ForceParams*, const int*, const int*, const int*, int, int,
+                                    int, bool, StateBuf<3>, const uint32_t*, StateBuf<3>, uint32_t*, uint32_t*,
+                                    uint32_t*, uint32_t*, const DebugOut*, int);
 
 template void launch_force<2>(cudaStream_t, const ForceParams&, bool, StateBuf<2>, const uint32_t*, StateBuf<2>,
                               uint32_t*, uint32_t*, uint32_t*, uint32_t*, const DebugOut*, int);

@@ -209,11 +209,16 @@ void launch_force(cudaStream_t st, const ForceParams& p, bool general, StateBuf<
 // nworlds + 1) the first tile of each world for this variant's tile size
 // (tile_targets), `tiles` the total.  Every world has nx >= 3.
 // smem_matrix: every world has at most 16 types.
+// steps_left (device, per world, may be null): a world at <= 0 is frozen
+// for the step (its state and order untouched, its cells counted again).
 template <int D>
 void launch_force_batch(cudaStream_t st, const ForceParams* worlds, const int* wp_off, const int* tile_off,
-                        int tiles, int nworlds, int n_total, bool smem_matrix, StateBuf<D> b, const uint32_t* cstart,
-                        StateBuf<D> a, uint32_t* cell, uint32_t* rank, uint32_t* counts, uint32_t* defer,
-                        const DebugOut* dbg, int variant = 0);
+                        const int* steps_left, int tiles, int nworlds, int n_total, bool smem_matrix, StateBuf<D> b,
+                        const uint32_t* cstart, StateBuf<D> a, uint32_t* cell, uint32_t* rank, uint32_t* counts,
+                        uint32_t* defer, const DebugOut* dbg, int variant = 0);
+
+// Counts every positive steps_left[k] (k < nworlds) down by one.
+void launch_batch_tick(cudaStream_t st, int* steps_left, int nworlds);
 
 // Targets per block of the force kernel's tile variant.
 int tile_targets(int dim, int variant);

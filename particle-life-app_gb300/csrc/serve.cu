@@ -3,14 +3,16 @@
 // world resident on the device, admits queued requests as memory and batch
 // slots free up, packs the active worlds into one batch per dimension (each
 // on its own stream, so the 2D and 3D batches overlap on the GPU), advances
-// them in chunks of steps, and hands back each world's final state.  This is
+// them in chunks of steps (a world whose own step count ends inside a chunk
+// freezes on the device until the chunk ends), and hands back each world's
+// final state.  This is
 // continuous batching: a request that arrives while others are running joins
 // at the next chunk boundary, and one that finishes leaves at it.
 //
 // Each result equals the world run alone: batched worlds do not interact and
 // the force kernel cuts every world into the same tiles whatever else is in
 // the batch, so a world's trajectory is bit for bit independent of the mix.
-// A chunk never takes a world past its own step count.
+// No world is ever stepped past its own step count.
 //
 // Latency is measured per request from plg_server_submit to the moment its
 // result is on the host.
@@ -182,6 +184,12 @@ int reshape(plg_server* s, int d) {
     int rc = plg_batch_update(b, (int32_t)removes.size(), removes.data(), (int32_t)descs.size(), descs.data(),
                               ids.data());
     if (rc) return fail_server(s, rc, std::string("batch update: ") + plg_batch_last_error(b));
+    for (size_t k = 0; k < admitted.size(); ++k) {
+        // The world freezes on the device once its own steps are done, so a
+        // chunk can be longer than its remaining steps.
+        rc = plg_batch_set_steps(b, ids[k], admitted[k]->remaining);
+        if (rc) return fail_server(s, rc, std::string("set steps: ") + plg_batch_last_error(b));
+    }
     std::lock_guard<std::mutex> lk(s->mu);
     for (size_t k = 0; k < admitted.size(); ++k) {
         admitted[k]->world = ids[k];
@@ -205,17 +213,18 @@ void scheduler(plg_server* s) {
         }
         for (int d = 0; d < 2; ++d)
             if (reshape(s, d)) return;
-        // One chunk: every active world advances k_d steps, both batches at
-        // once; k_d never exceeds a world's remaining steps (a world with none
-        // left, e.g. a 0-step request, is handed back by the next reshape).
+        // One chunk: up to max_chunk_steps batch steps, both batches at once
+        // (each on its own stream).  A world whose own steps run out inside
+        // the chunk freezes on the device; the next reshape hands it back.
         int32_t k[2] = {0, 0};
         bool pending = false;
         for (int d = 0; d < 2; ++d) {
-            if (s->active[d].empty()) continue;
-            int32_t m = s->cfg.max_chunk_steps;
-            for (auto& r : s->active[d]) m = std::min(m, r->remaining);
-            k[d] = m;
-            pending |= m == 0;
+            int32_t m = 0;
+            for (auto& r : s->active[d]) {
+                m = std::max(m, r->remaining);
+                pending |= r->remaining == 0;
+            }
+            k[d] = std::min(m, s->cfg.max_chunk_steps);
         }
         if (!k[0] && !k[1]) {
             if (pending) continue;
@@ -233,8 +242,9 @@ void scheduler(plg_server* s) {
             if (plg_batch_sync(s->batch[d], 0.0))
                 return (void)fail_server(s, PLG_E_DEVICE, std::string("sync: ") + plg_batch_last_error(s->batch[d]));
             for (auto& r : s->active[d]) {
-                r->remaining -= k[d];
-                ps += (double)r->n * k[d];
+                const int32_t done = std::min(r->remaining, k[d]);
+                r->remaining -= done;
+                ps += (double)r->n * done;
             }
         }
         std::lock_guard<std::mutex> lk(s->mu);

@@ -149,6 +149,8 @@ SIGNATURES = {
     "plg_batch_set_tile": (C.c_int, [_P, C.c_int32]),
     "plg_batch_get_tile": (C.c_int, [_P, _I32P]),
     "plg_batch_autotune": (C.c_int, [_P, C.c_int32, _I32P, _DP]),
+    "plg_batch_set_steps": (C.c_int, [_P, C.c_int32, C.c_int32]),
+    "plg_batch_steps_left": (C.c_int, [_P, C.c_int32, _I32P]),
     "plg_world_check": (C.c_int, [C.c_int32, C.POINTER(plg_world_desc)]),
     "plg_world_device_bytes": (C.c_int64, [C.c_int32, C.POINTER(plg_world_desc)]),
     "plg_server_create": (C.c_int, [C.POINTER(plg_server_config), C.POINTER(_P)]),

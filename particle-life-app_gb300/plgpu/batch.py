@@ -143,6 +143,15 @@ class GpuBatch:
         out["cell"] = out["cell"] - c
         return out
 
+    def set_steps(self, wid: int, steps: int) -> None:
+        """The world freezes after `steps` more batch steps (< 0: no limit)."""
+        _check(self.lib.plg_batch_set_steps(self.b, wid, steps), self.b, "plg_batch_set_steps")
+
+    def steps_left(self, wid: int) -> int:
+        v = _lib.C.c_int32()
+        _check(self.lib.plg_batch_steps_left(self.b, wid, _lib.C.byref(v)), self.b, "plg_batch_steps_left")
+        return v.value
+
     def set_tile(self, variant: int) -> None:
         _check(self.lib.plg_batch_set_tile(self.b, variant), self.b, "plg_batch_set_tile")
 

@@ -180,3 +180,27 @@ def test_dense_world_alone_and_in_a_mix_is_bit_identical(gpu):
     mix.close()
     for a, c in zip(ref, got):
         assert np.array_equal(a, c)
+
+
+def test_step_budget_freezes_a_world(gpu):
+    """A world whose step budget runs out keeps its state while the others
+    advance, and continues exactly where it stopped."""
+    specs = mixed_2d_specs()[:3]
+    ref3 = []
+    for spec, n in ((specs[1], 3), (specs[1], 5), (specs[0], 7)):
+        b1, (w1,) = make_batch(2, [spec])
+        ref3.append(trajectory(b1, w1, n))
+        b1.close()
+    b, ids = make_batch(2, specs)
+    b.set_steps(ids[1], 3)
+    b.step(7)
+    assert b.steps_left(ids[1]) == 0 and b.steps_left(ids[0]) == -1
+    for x, y in zip(b.download(ids[1]), ref3[0]):
+        assert np.array_equal(x, y)
+    for x, y in zip(b.download(ids[0]), ref3[2]):
+        assert np.array_equal(x, y)
+    b.set_steps(ids[1], -1)
+    b.step(2)
+    for x, y in zip(b.download(ids[1]), ref3[1]):
+        assert np.array_equal(x, y)
+    b.close()
