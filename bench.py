@@ -16,6 +16,10 @@ Our arm (default):
          events over a profiled pass of the same steps.
   cpu_baseline  the oracle (C FP64 restatement of the reference's step, all
          host threads) on a bounded sample of steps of the same workload.
+  batched  512 uneven 2D worlds through plg_batch_* (autotuned) against the
+         same worlds one at a time through single-world contexts.
+  serving  Poisson request arrivals through plg_server_* (scaled sizes, see
+         run_serving), completion latency p50/p99 and delivered throughput.
 --impl reference: the same workload through the oracle port on all host
 cores (the reference is Java and no JDK exists on either machine).
 
