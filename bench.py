@@ -16,6 +16,7 @@ Our arm (default):
          events over a profiled pass of the same steps.
   cpu_baseline  the oracle (C FP64 restatement of the reference's step, all
          host threads) on a bounded sample of steps of the same workload.
+  blobs_3d  the 4M-particle 3D blob world (uneven cells), device-resident.
   batched  512 uneven 2D worlds through plg_batch_* (autotuned) against the
          same worlds one at a time through single-world contexts.
   serving  Poisson request arrivals through plg_server_* (scaled sizes, see
@@ -69,6 +70,8 @@ def parse():
     ap.add_argument("--batched-worlds", type=int, default=512)
     ap.add_argument("--batched-steps", type=int, default=20)
     ap.add_argument("--no-serving", action="store_true", help="skip the serving measurement")
+    ap.add_argument("--no-3d", action="store_true", help="skip the 3D blob measurement")
+    ap.add_argument("--steps-3d", type=int, default=20)
     ap.add_argument("--serve-seconds", type=float, default=10.0)
     ap.add_argument("--serve-rate", type=float, default=200.0)
     return ap.parse_args()
@@ -203,6 +206,58 @@ def run_batched(args) -> dict:
             "autotune": {"chosen_tile_variant": variant, "ms_per_step_by_variant": tune_ms},
             "config": "512 2D periodic worlds, N log-uniform [1e3, 2e5], types 3..12, rmax U[0.005, 0.03] "
                       "(unit box), friction t1/2 U[0.02, 0.1] s, dt 0.02; seeded Philox"}
+
+
+def run_blobs_3d(args) -> dict:
+    """The 3D configuration: 4M particles in 64 Gaussian blobs (uneven cell
+    occupancy), 16 types, about 40 neighbours, one world, device-resident."""
+    import torch
+
+    from plgpu import _lib, workloads
+    from plgpu.physics import GpuWorld
+
+    w = workloads.blob_world_3d()
+    n = w.pos.shape[0]
+    g = GpuWorld(3, n)
+    g.set_settings(w.rmax, w.friction, w.force, w.dt, beta=w.beta, wrap=w.wrap)
+    g.set_matrix(w.matrix)
+    g.upload(w.pos, None, w.types)
+    stream = torch.cuda.ExternalStream(g.stream())
+    g.step(args.warmup)
+    lib = _lib.load()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps_3d)]
+    torch.cuda.synchronize()
+    for k in range(args.steps_3d):  # state 2 x 128 MB > L2: no flush needed
+        ev[k][0].record(stream)
+        plgpu_check(lib.plg_step_async(g.ctx, 1), g.ctx, "plg_step_async")
+        ev[k][1].record(stream)
+    plgpu_check(lib.plg_sync(g.ctx, 120.0), g.ctx, "plg_sync")
+    ms = np.array([a.elapsed_time(b) for a, b in ev])
+    lib.plg_profile_enable(g.ctx, 1)
+    g.step(5)
+    kern = {}
+    for k, name in enumerate(_lib.KERNELS):
+        t = _lib.C.c_double()
+        c = _lib.C.c_int64()
+        lib.plg_profile_read(g.ctx, k, _lib.C.byref(t), _lib.C.byref(c))
+        kern[name] = {"avg_us": 1e3 * t.value / max(c.value, 1), "launches": c.value}
+    lib.plg_profile_enable(g.ctx, 0)
+    deferred = g.deferred()
+    dbg = g.debug_step()
+    g.close()
+    cand = dbg["candidates"] / n
+    inter = float(dbg["pairs"].mean())
+    return {"metric": "particle-steps/s, 3D blobs", "value": n * len(ms) / (ms.sum() * 1e-3), "unit": UNIT,
+            "ms_per_step": float(ms.mean()), "kernels": kern, "deferred_targets_last_step": deferred,
+            "candidates_per_particle": cand, "interactions_per_particle": inter,
+            "config": f"3D periodic unit cube, N={n}, 64 Gaussian blobs sigma 0.025 (0.05 in [-1,1]^3), 16 types, "
+                      f"rmax {w.rmax} (mean 40 neighbours), dt 0.01; seeded Philox"}
+
+
+def plgpu_check(status, ctx, what):
+    import plgpu.physics
+
+    plgpu.physics.check(status, ctx, what)
 
 
 def run_serving(args) -> dict:
@@ -427,6 +482,9 @@ def run_ours(args):
             gbs = b / (kern[name]["avg_us"] * 1e-6) / 1e9
             sort_kernels[name] = {"achieved_gbs": gbs, "frac_of_measured_hbm": gbs / hbm}
 
+    blobs3d = None
+    if rank == 0 and not args.no_3d:
+        blobs3d = run_blobs_3d(args)
     batched = None
     if rank == 0 and not args.no_batched:
         batched = run_batched(args)
@@ -465,6 +523,7 @@ def run_ours(args):
             "candidates_per_particle": cand,
             "interactions_per_particle": inter,
             "cpu_baseline": cpu,
+            "blobs_3d": blobs3d,
             "batched": batched,
             "serving": serving,
             "clocks": clk,

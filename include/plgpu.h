@@ -188,8 +188,8 @@ int plg_debug_step(plg_ctx* ctx, int32_t* cell, int32_t* pairs,
                    int64_t* candidates);
 
 /* Targets of the last step that the tiled force kernel recomputed in its
- * closing global-memory pass (pairs needing the FP64 decision, or stencils
- * too large for shared memory).  Waits for the context's stream. */
+ * closing global-memory pass (targets with a pair that needs the FP64
+ * decision).  Waits for the context's stream. */
 int plg_step_stats(plg_ctx* ctx, int64_t* deferred);
 
 /* Device FP32 FMA throughput microbenchmark on the current device, in

@@ -15,10 +15,12 @@
 // segment's stencil (3 rows in 2D, 9 in 3D, over the segment's columns plus a
 // halo column each side) column by column, so that the whole neighbourhood of
 // a target in column cx is one contiguous run (columns cx-1..cx+1).  The
-// candidate loop is branch-free FP32.  A target that meets a candidate needing
-// the FP64 decision, or whose segment does not fit in shared memory, is
-// deferred: at the end of the block one warp recomputes it from global
-// memory (fixup_target).
+// candidate loop is branch-free FP32.  A segment that does not fit in shared
+// memory (a sparse row spanning many columns, or a very dense region) is
+// computed from global memory in the same candidate order (direct_stencil),
+// giving the same bits.  A target that meets a candidate needing the FP64
+// decision is deferred: at the end of the block one warp recomputes it from
+// global memory (fixup_target).
 //
 // Pair test.  The reference keeps a pair when d2 != 0 && d2 <= rmax*rmax in
 // FP64, with d = wrapConnection(q - p) (Physics.java:428-432).  Here d2 is
@@ -633,15 +635,52 @@ __device__ __forceinline__ float rsqrt_approx(float x) {
 // true: the caller then defers the target to the FP64 fixup, which discards
 // this partial sum.  SHIFT: the segment touches the box's upper boundary,
 // so some candidates carry target-shift flags.
+// Loop constants of the candidate evaluation, read once into registers
+// (otherwise the compiler re-reads them from the parameter bank per
+// candidate).
+struct LoopK {
+    float lo, hi, tiny, m2, opb, iomb, brm, k1;
+    __device__ __forceinline__ explicit LoopK(const ForceParams& P)
+        : lo(P.lo), hi(P.hi), tiny(P.tiny), m2(P.m2_inv_rmax), opb(P.one_plus_beta),
+          iomb(P.inv_one_minus_beta), brm(P.beta_rmax), k1(P.k1) {}
+};
+
+// One candidate: d = q - p with the image shifts already applied to q and p,
+// the FP32 Accelerator term added to acc, band / tiny pairs flagged in rare.
+// The staged and the direct paths both use it, in the same candidate order,
+// so they produce the same bits.  Returns d2.
+template <int D>
+__device__ __forceinline__ float eval_candidate(const LoopK& K, float qx, float qy, float qz, float pxe, float pye,
+                                                float pze, float a, Acc& acc, bool& rare) {
+    const float dx = qx - pxe;
+    const float dy = qy - pye;
+    float d2;
+    float dz = 0.f;
+    if (D == 3) {
+        dz = qz - pze;
+        d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+    } else {
+        d2 = fmaf(dx, dx, dy * dy);
+    }
+    rare |= ((d2 > K.lo) & (d2 < K.hi)) | (d2 < K.tiny);
+    const float inv = rsqrt_approx(d2);
+    const float dist = d2 * inv;
+    const float t = fmaf(dist, K.m2, K.opb);
+    const float u = fmaxf(fmaf(-fabsf(t), K.iomb, 1.f), 0.f);
+    const float g = dist < K.brm ? K.k1 - inv : (a * inv) * u;
+    acc.x = fmaf(dx, g, acc.x);
+    acc.y = fmaf(dy, g, acc.y);
+    if (D == 3) acc.z = fmaf(dz, g, acc.z);
+    return d2;
+}
+
 template <int D, bool DBG, bool SHIFT, int V>
 __device__ __forceinline__ bool tile_range(const ForceArgs<D>& A, const ForceParams& P, const TileSmem<D, V>& sm,
                                            const float* __restrict__ Mrow, int ncell, int ja, int jb, float px,
                                            float py, float pz, Acc& acc) {
     const float px1 = px - 1.f, py1 = py - 1.f, pz1 = pz - 1.f;
     bool rare = false;
-    // Loop constants in registers (read once, not per candidate).
-    const float c_lo = P.lo, c_hi = P.hi, c_tiny = P.tiny, c_m2 = P.m2_inv_rmax, c_opb = P.one_plus_beta;
-    const float c_iomb = P.inv_one_minus_beta, c_brm = P.beta_rmax, c_k1 = P.k1;
+    const LoopK K(P);
     for (int j = ja; j < jb; ++j) {
         const float4 q = sm.cand[j];
         int tb = __float_as_int(D == 3 ? q.w : q.z);
@@ -652,30 +691,78 @@ __device__ __forceinline__ bool tile_range(const ForceArgs<D>& A, const ForcePar
             if (D == 3) pze = (tb & kShiftZ) ? pz1 : pz;
             tb &= 0xffff;
         }
-        const float dx = q.x - pxe;
-        const float dy = q.y - pye;
-        float d2;
-        float dz = 0.f;
-        if (D == 3) {
-            dz = q.z - pze;
-            d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-        } else {
-            d2 = fmaf(dx, dx, dy * dy);
-        }
-        rare |= ((d2 > c_lo) & (d2 < c_hi)) | (d2 < c_tiny);
-        const float a = Mrow[tb];
-        const float inv = rsqrt_approx(d2);
-        const float dist = d2 * inv;
-        const float t = fmaf(dist, c_m2, c_opb);
-        const float u = fmaxf(fmaf(-fabsf(t), c_iomb, 1.f), 0.f);
-        const float g = dist < c_brm ? c_k1 - inv : (a * inv) * u;
-        acc.x = fmaf(dx, g, acc.x);
-        acc.y = fmaf(dy, g, acc.y);
-        if (D == 3) acc.z = fmaf(dz, g, acc.z);
+        const float d2 = eval_candidate<D>(K, q.x, q.y, q.z, pxe, pye, pze, Mrow[tb], acc, rare);
         if (DBG) {
             acc.cand++;
-            if ((d2 <= c_lo) & (d2 >= c_tiny))
+            if ((d2 <= K.lo) & (d2 >= K.tiny))
                 add_pair<D, true>(acc, make_float4(0.f, 0.f, 0.f, 0.f), id_of<D>(A, staged_global(sm, ncell, j)));
+        }
+    }
+    return rare;
+}
+
+// The target's neighbourhood read straight from global memory, for segments
+// too wide or too full for shared memory: the cells in the staged order
+// (columns cx-1..cx+1, and in each the R stencil rows), the same image
+// shifts (below the box: the candidate's coordinate minus 1; above: the
+// target's) and the same candidate evaluation, so the sum has the same bits
+// as the staged path would give.
+template <int D, bool DBG>
+__device__ __noinline__ bool direct_stencil(const ForceArgs<D>& A, const ForceParams& P,
+                                            const uint32_t* __restrict__ cs, const float* __restrict__ Mrow, int s,
+                                            float px, float py, float pz, int cx, int cy, int cz, Acc& acc) {
+    constexpr int R = D == 3 ? 9 : 3;
+    const LoopK K(P);
+    const int nx = P.g.nx;
+    const bool wrap = P.wrap != 0;
+    bool rare = false;
+    for (int ci = 0; ci < 3; ++ci) {
+        int col = cx - 1 + ci;
+        bool qsx = false, tsx = false;
+        if (col < 0) {
+            col += nx;
+            qsx = wrap;
+        } else if (col >= nx) {
+            col -= nx;
+            tsx = wrap;
+        }
+        const float pxe = tsx ? px - 1.f : px;
+        for (int r = 0; r < R; ++r) {
+            int ry = cy + r % 3 - 1, rz = D == 3 ? cz + r / 3 - 1 : 0;
+            bool qsy = false, qsz = false;
+            float pye = py, pze = pz;
+            if (ry < 0) {
+                ry += nx;
+                qsy = wrap;
+            } else if (ry >= nx) {
+                ry -= nx;
+                if (wrap) pye = py - 1.f;
+            }
+            if (D == 3) {
+                if (rz < 0) {
+                    rz += nx;
+                    qsz = wrap;
+                } else if (rz >= nx) {
+                    rz -= nx;
+                    if (wrap) pze = pz - 1.f;
+                }
+            }
+            const int c = (rz * nx + ry) * nx + col;
+            const int j0 = (int)__ldg(cs + c), j1 = (int)__ldg(cs + c + 1);
+            for (int j = j0; j < j1; ++j) {
+                if (j == s) continue;
+                float4 q = __ldg(A.bpt + j);
+                if (qsx) q.x -= 1.f;
+                if (qsy) q.y -= 1.f;
+                if (D == 3 && qsz) q.z -= 1.f;
+                const float d2 = eval_candidate<D>(K, q.x, q.y, q.z, pxe, pye, pze, Mrow[Layout<D>::type(q)], acc,
+                                                   rare);
+                if (DBG) {
+                    acc.cand++;
+                    if ((d2 <= K.lo) & (d2 >= K.tiny))
+                        add_pair<D, true>(acc, make_float4(0.f, 0.f, 0.f, 0.f), id_of<D>(A, j));
+                }
+            }
         }
     }
     return rare;
@@ -718,12 +805,13 @@ __device__ __noinline__ void fixup_target(const ForceArgs<D>& A, const ForcePara
     }
 }
 
-// Main force kernel (nx >= 3): one thread per target; a block takes 256 (3D: 128)
-// consecutive targets and, per segment (targets of one grid row), stages the segment's stencil so that each target reads one
-// contiguous run.  FP32 only and call-free: a target whose run meets a
-// candidate that needs the FP64 decision, or whose segment did not fit in
-// shared memory, is deferred to the block's closing pass (fixup_target),
-// which recomputes it completely.
+// Main force kernel (nx >= 3): one thread per target; a block takes 256 (3D:
+// 128) consecutive targets and, per segment (targets of one grid row), stages
+// the segment's stencil so that each target reads one contiguous run (or,
+// when the segment does not fit, reads the same cells from global memory).
+// FP32 only: a target whose neighbourhood holds a candidate that needs the
+// FP64 decision is deferred to the block's closing pass (fixup_target), which
+// recomputes it completely.
 // BATCH: the sorted order holds many worlds one after another (their cells
 // are disjoint ranges of one global cell index).  Tiles are laid out per
 // world: block b works on tile b - tile_off[k] of the world k that owns it,
@@ -800,7 +888,7 @@ __global__ void __launch_bounds__(TileCfg<D, V>::kTargets, TileCfg<D, V>::kMinBl
     const float px = me.x, py = me.y, pz = D == 3 ? me.z : 0.f;
     const float* Mrow = M + (valid ? Layout<D>::type(me) : 0) * P.ntypes;
     Acc acc = {0.f, 0.f, 0.f, 0, 0ull, 0ull, 0ull};
-    bool defer = false;
+    bool defer = false, direct = false;
     for (int g = 0; g < nseg; ++g) {
         const int ta = sm.seg[g], tb = sm.seg[g + 1];
         const int srow = sm.rowid[ta];
@@ -825,10 +913,16 @@ __global__ void __launch_bounds__(TileCfg<D, V>::kTargets, TileCfg<D, V>::kMinBl
                     defer |= tile_range<D, DBG, false, V>(A, P, sm, Mrow, ncell, self_j + 1, j1, px, py, pz, acc);
                 }
             } else {
-                defer = true;
+                direct = true;  // computed after the loop, off the hot path
             }
         }
         if (g + 1 < nseg) __syncthreads();  // staging of the next segment reuses smem
+    }
+    if (direct) {
+        // The segment did not fit in shared memory: the same sum from
+        // global memory.
+        const int cy = axis_cell(py, P.g), cz = D == 3 ? axis_cell(pz, P.g) : 0;
+        defer = direct_stencil<D, DBG>(A, P, A.cstart + P.cell_base, Mrow, s, px, py, pz, cx, cy, cz, acc);
     }
     const bool done = valid && !defer;
     uint32_t newcell = 0;
@@ -838,8 +932,8 @@ __global__ void __launch_bounds__(TileCfg<D, V>::kTargets, TileCfg<D, V>::kMinBl
         A.rank[s] = bin_count(A.counts, newcell, mask);
         A.cell[s] = newcell;
     }
-    // Deferred targets of this block (FP64 band pairs, overfull segments),
-    // one warp each, from global memory.  Most blocks have none.
+    // Deferred targets of this block (FP64 band pairs), one warp each, from
+    // global memory.  Most blocks have none.
     const int warp = tid >> 5, lane = tid & 31;
     const unsigned dm = __ballot_sync(kFull, valid && defer);
     __syncthreads();  // rowid and wsum are free again

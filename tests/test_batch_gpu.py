@@ -166,14 +166,13 @@ def test_autotune_restores_state_and_variants_agree(gpu):
 
 
 def test_dense_world_alone_and_in_a_mix_is_bit_identical(gpu):
-    """Dense worlds overflow the shared-memory staging and take the deferred
-    path for some targets; tiles are laid out per world, so the same targets
-    defer alone and in a mix."""
+    """Dense worlds overflow the shared-memory staging; tiles are laid out per
+    world, so the same segments take the global-memory path alone and in a
+    mix."""
     dense = uniform_world(60_000, 5, 0.05, seed=81, vel_scale=0.01)  # 150 per cell: segments overflow
     others = [uniform_world(7_777, 4, 0.02, seed=82), uniform_world(3_001, 3, 0.04, seed=83)]
     alone, (aid,) = make_batch(2, [dense])
     ref = trajectory(alone, aid, 3)
-    assert alone.deferred() > 0
     alone.close()
     mix, ids = make_batch(2, others[:1] + [dense] + others[1:])
     got = trajectory(mix, ids[1], 3)

@@ -129,8 +129,8 @@ def test_deferred_targets_are_rare_for_uniform_worlds(gpu):
 
 
 def test_2d_dense_clusters_overflow_shared_memory(gpu):
-    """Clusters far denser than shared memory can stage: those targets take
-    the deferred (global-memory) path."""
+    """Clusters far denser than shared memory can stage: those segments are
+    computed from global memory in the staged order."""
     spec = blob_world(60_000, 5, 0.01, nblobs=12, sigma=0.004, seed=14, dim=2)
     r = check_step(spec, gpu)
     assert r["pairs"] > 100
@@ -149,3 +149,29 @@ def test_empty_and_single(gpu):
     check_step(uniform_world(0, 3, 0.05, seed=13), gpu)
     check_step(uniform_world(1, 3, 0.05, seed=13), gpu)
     check_step(uniform_world(2, 3, 0.5, seed=13), gpu)
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_staged_and_global_memory_paths_agree(gpu, dim):
+    """A world whose segments overflow shared memory under one tile variant
+    and fit under the other: the staged and the global-memory paths walk the
+    same candidates in the same order, so the two runs agree bit for bit."""
+    from plgpu.batch import GpuBatch, WorldDesc
+
+    # ~115 per cell (2D) and ~20 per cell (3D): a 128-target tile overflows
+    # variant 1's staging (1024 / 1280 candidates), a tile of variant 0
+    # (1536 / 2560) mostly fits.
+    spec = (uniform_world(46_000, 5, 0.05, seed=17, vel_scale=0.01) if dim == 2 else
+            uniform_world(20_000, 6, 0.1, seed=18, dim=3, vel_scale=0.01))
+    runs = []
+    for variant in (0, 1):
+        b = GpuBatch(dim, spec.n + 1, 4, int(np.floor(1 / spec.rmax)) ** dim + 1)
+        (wid,) = b.update(add=[WorldDesc(pos=spec.pos, types=spec.types, matrix=spec.matrix, rmax=spec.rmax,
+                                         friction=spec.friction, force=spec.force, dt=spec.dt, beta=spec.beta,
+                                         wrap=spec.wrap, vel=spec.vel)])
+        b.set_tile(variant)
+        b.step(3)
+        runs.append(b.download(wid))
+        b.close()
+    for a, c in zip(*runs):
+        assert np.array_equal(a, c)
