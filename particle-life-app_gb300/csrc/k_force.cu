@@ -462,11 +462,11 @@ struct TileCfg<2, 1> {
 };
 template <>
 struct TileCfg<3, 0> {
-    static constexpr int kTargets = 128, kMinBlocks = 4, kCap = 2560, kCells = 512;
+    static constexpr int kTargets = 128, kMinBlocks = 6, kCap = 1536, kCells = 512;
 };
 template <>
 struct TileCfg<3, 1> {
-    static constexpr int kTargets = 128, kMinBlocks = 5, kCap = 1280, kCells = 512;
+    static constexpr int kTargets = 64, kMinBlocks = 10, kCap = 1024, kCells = 384;
 };
 
 // Target shifts a staged candidate asks for (bits 16..18 of its type word):
@@ -474,7 +474,7 @@ struct TileCfg<3, 1> {
 // the periodic image above the box of a cell near coordinate 0.
 constexpr int kShiftX = 1 << 16, kShiftY = 1 << 17, kShiftZ = 1 << 18;
 
-// Lives in dynamic shared memory (variant 0: about 31 KB in 2D, 47 KB in 3D).
+// Lives in dynamic shared memory (variant 0: about 31 KB in 2D, 31 KB in 3D).
 template <int D, int V>
 struct TileSmem {
     float4 cand[TileCfg<D, V>::kCap];      // staged candidates, column-major by stencil cell

@@ -160,9 +160,9 @@ def test_autotune_restores_state_and_variants_agree(gpu):
         bb.step(4)
         runs.append([bb.download(w) for w in ii])
         bb.close()
-    for r0, r1 in zip(*runs):
-        assert np.array_equal(r0[3], r1[3])
-        np.testing.assert_allclose(r0[0], r1[0], rtol=0, atol=1e-6)
+    for r0, r1 in zip(*runs):  # tile variants give the same bits
+        for a, c in zip(r0, r1):
+            assert np.array_equal(a, c)
 
 
 def test_dense_world_alone_and_in_a_mix_is_bit_identical(gpu):
