@@ -141,6 +141,46 @@ int plg_download(plg_ctx* ctx, double* pos, double* vel, int32_t* type,
 
 int plg_particle_count(plg_ctx* ctx, int64_t* n);
 
+/* ---- edits on the device (no re-upload) --------------------------------- */
+
+/* A cursor of app/cursors/Cursor.java:10-13: position, size and shape
+ * (CircleCursorShape, SquareCursorShape, InfinityCursorShape).  A particle
+ * is inside when its delta to the cursor (wrapped when settings.wrap),
+ * divided by size, passes the shape's test (Cursor.java:16-35). */
+#define PLG_CURSOR_CIRCLE 0
+#define PLG_CURSOR_SQUARE 1
+#define PLG_CURSOR_INFINITY 2
+typedef struct plg_cursor {
+    double x, y, z;
+    double size;
+    int32_t shape;
+    int32_t reserved;
+} plg_cursor;
+
+/* Cursor.countSelection (Cursor.java:44-50). */
+int plg_cursor_count(plg_ctx* ctx, const plg_cursor* cursor, int64_t* count);
+/* Cursor action MOVE (app/Main.java:540-551): every selected particle moves
+ * by (dx, dy, dz) and is wrapped or clamped (ensurePosition). */
+int plg_cursor_move(plg_ctx* ctx, const plg_cursor* cursor, double dx, double dy, double dz,
+                    int64_t* moved);
+/* Cursor action DELETE (app/Main.java:567-578): the unselected particles
+ * stay, in their order. */
+int plg_cursor_delete(plg_ctx* ctx, const plg_cursor* cursor, int64_t* deleted);
+/* Appends particles at the end (cursor action BRUSH, app/Main.java:552-566;
+ * growth in Physics.setParticleCount, Physics.java:212-219), in the
+ * plg_upload layouts.  Their ids continue after every id handed out so
+ * far. */
+int plg_append(plg_ctx* ctx, int64_t n, const double* pos, const double* vel,
+               const int32_t* type);
+/* Reorders and truncates: particle k becomes the old particle src[k]
+ * (k < n_new, distinct indices of the current order).  The shuffle and
+ * truncation of Physics.setParticleCount (Physics.java:200-211) and of
+ * ExtendedPhysics.setTypeCount (app/ExtendedPhysics.java:41-130). */
+int plg_permute(plg_ctx* ctx, int64_t n_new, const int32_t* src);
+/* New types for all particles, in the current order (Physics.ensureTypes,
+ * setTypes: Physics.java:266-272, 509-511). */
+int plg_set_types(plg_ctx* ctx, const int32_t* type);
+
 /* Thread-safe stop request: Physics.forceUpdateStop (Physics.java:149-151)
  * and Physics.kill (Physics.java:156-158).  Takes effect between steps. */
 int plg_request_stop(plg_ctx* ctx);

@@ -63,7 +63,8 @@ __global__ void __launch_bounds__(kThreads) k_upload(int n, const double* __rest
                                                      const int32_t* __restrict__ type, int ntypes,
                                                      StateBuf<D> a, uint32_t* __restrict__ cell,
                                                      uint32_t* __restrict__ rank, uint32_t* counts, Grid g,
-                                                     uint32_t* status, bool vec, uint32_t cell_base) {
+                                                     uint32_t* status, bool vec, uint32_t cell_base,
+                                                     int id_base) {
     __shared__ __align__(16) double sp[3 * kThreads];
     __shared__ __align__(16) double sv[3 * kThreads];
     const int i0 = blockIdx.x * kThreads;
@@ -105,11 +106,11 @@ __global__ void __launch_bounds__(kThreads) k_upload(int n, const double* __rest
             ty = 0;
         }
         if constexpr (D == 2) {
-            a.pt[i] = make_float4(p[0], p[1], __int_as_float(ty), __int_as_float(i));
+            a.pt[i] = make_float4(p[0], p[1], __int_as_float(ty), __int_as_float(id_base + i));
             reinterpret_cast<float2*>(a.vel)[i] = make_float2(v[0], v[1]);
         } else {
             a.pt[i] = make_float4(p[0], p[1], p[2], __int_as_float(ty));
-            reinterpret_cast<float4*>(a.vel)[i] = make_float4(v[0], v[1], v[2], __int_as_float(i));
+            reinterpret_cast<float4*>(a.vel)[i] = make_float4(v[0], v[1], v[2], __int_as_float(id_base + i));
         }
         c = cell_base + cell_index<D>(p[0], p[1], p[2], g);
         if (bad) atomicOr(status, bad);
@@ -392,11 +393,11 @@ inline bool aligned16(const void* p) { return ((uintptr_t)p & 15u) == 0; }
 template <int D>
 void launch_upload(cudaStream_t st, int n, const double* pos, const double* vel, const int32_t* type, int ntypes,
                    StateBuf<D> a, uint32_t* cell, uint32_t* rank, uint32_t* counts, Grid g, uint32_t* status,
-                   uint32_t cell_base) {
+                   uint32_t cell_base, int id_base) {
     if (n <= 0) return;
     const bool vec = aligned16(pos) && aligned16(vel);
     k_upload<D><<<blocks_for(n, kThreads), kThreads, 0, st>>>(n, pos, vel, type, ntypes, a, cell, rank, counts, g,
-                                                              status, vec, cell_base);
+                                                              status, vec, cell_base, id_base);
 }
 
 template <int D>
@@ -459,9 +460,9 @@ void launch_gather(cudaStream_t st, int n, const uint32_t* perm, const uint32_t*
 }
 
 template void launch_upload<2>(cudaStream_t, int, const double*, const double*, const int32_t*, int, StateBuf<2>,
-                               uint32_t*, uint32_t*, uint32_t*, Grid, uint32_t*, uint32_t);
+                               uint32_t*, uint32_t*, uint32_t*, Grid, uint32_t*, uint32_t, int);
 template void launch_upload<3>(cudaStream_t, int, const double*, const double*, const int32_t*, int, StateBuf<3>,
-                               uint32_t*, uint32_t*, uint32_t*, Grid, uint32_t*, uint32_t);
+                               uint32_t*, uint32_t*, uint32_t*, Grid, uint32_t*, uint32_t, int);
 template void launch_rebin<2>(cudaStream_t, int, StateBuf<2>, uint32_t*, uint32_t*, uint32_t*, Grid);
 template void launch_rebin<3>(cudaStream_t, int, StateBuf<3>, uint32_t*, uint32_t*, uint32_t*, Grid);
 template void launch_download<2>(cudaStream_t, int, StateBuf<2>, double*, double*, int32_t*, int32_t*);

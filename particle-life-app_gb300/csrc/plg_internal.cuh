@@ -23,6 +23,16 @@ enum DeviceStatus : uint32_t {
     kDevBadType = 1u << 1,      // upload: type outside [0, matrix size)
     kDevBadVelocity = 1u << 2,  // upload: velocity not finite
     kDevSpinLimit = 1u << 3,    // a bounded device wait ran out
+    kDevBadIndex = 1u << 4,     // permute: source index outside the particles
+};
+
+// Cursor shapes of app/cursors (CircleCursorShape, SquareCursorShape,
+// InfinityCursorShape) and a cursor as the device kernels see it.
+constexpr int kCursorCircle = 0, kCursorSquare = 1, kCursorInfinity = 2;
+struct CursorDev {
+    double x, y, z, size;
+    int shape;
+    int wrap;
 };
 
 template <int D>
@@ -155,11 +165,32 @@ struct StateBuf {
 
 // ---- launchers (defined in the .cu files, called by the host library) ----
 
-// cell_base: added to every cell index (a world's first cell in a batch).
+// cell_base: added to every cell index (a world's first cell in a batch);
+// id_base: the id of the first particle (ids are id_base + index).
 template <int D>
 void launch_upload(cudaStream_t st, int n, const double* pos, const double* vel, const int32_t* type,
                    int ntypes, StateBuf<D> a, uint32_t* cell, uint32_t* rank, uint32_t* counts, Grid g,
-                   uint32_t* status, uint32_t cell_base = 0);
+                   uint32_t* status, uint32_t cell_base = 0, int id_base = 0);
+
+// ---- device-side edits (k_edit.cu) ----
+// flag[i] = particle i inside the cursor; *count += the number inside.
+template <int D>
+void launch_cursor_mark(cudaStream_t st, int n, const float4* pt, const CursorDev& cu, uint32_t* flag,
+                        unsigned long long* count);
+// Flagged particles move by (dx, dy, dz) (FP64), then wrap or clamp.
+template <int D>
+void launch_cursor_move(cudaStream_t st, int n, float4* pt, const uint32_t* flag, double dx, double dy, double dz,
+                        int wrap);
+void launch_invert(cudaStream_t st, int n, uint32_t* flag);
+// b[off[i]] = a[i] for every i with off[i + 1] > off[i].
+template <int D>
+void launch_compact(cudaStream_t st, int n, const uint32_t* off, StateBuf<D> a, StateBuf<D> b);
+// b[k] = a[src[k]] for k < n (src on the device, values in [0, n_old)).
+template <int D>
+void launch_permute(cudaStream_t st, int n, const int32_t* src, int n_old, StateBuf<D> a, StateBuf<D> b,
+                    uint32_t* status);
+template <int D>
+void launch_set_types(cudaStream_t st, int n, const int32_t* type, int ntypes, float4* pt, uint32_t* status);
 
 // Batched worlds: copies surviving worlds to their new places,
 // b[s] = a[old_off[k] + s - new_off[k]] for new_off[k] <= s < new_off[k + 1]

@@ -110,6 +110,7 @@ struct plg_ctx {
     int dim = 2;
     int64_t cap = 0;
     int64_t n = 0;
+    int64_t next_id = 0;  // id of the next particle added (plg_append)
     int device = 0;
     cudaStream_t stream = nullptr;
 
@@ -152,6 +153,13 @@ struct plg_ctx {
 
     uint32_t* status_d = nullptr;
     uint32_t* status_h = nullptr;
+
+    // device-side edits (allocated on first use)
+    uint32_t* edit_flag = nullptr;       // cap: marks / host indices / types
+    uint32_t* edit_off = nullptr;        // cap + 1: exclusive scan of the marks
+    unsigned long long* edit_scan = nullptr;
+    unsigned long long* edit_cnt = nullptr;
+    int64_t edit_cap = 0, edit_scan_cap = 0;
 
     // instrumented step
     int32_t* dbg_pairs = nullptr;
@@ -390,7 +398,8 @@ int free_all(plg_ctx* c) {
     void* ptrs[] = {c->bounds,    c->counts,   c->cstart,   c->scan_state, c->matrix,   c->apt,
                     c->bpt,       c->avel,     c->bvel,     c->cell,       c->rank,     c->perm,
                     c->slot_cell, c->defer,    c->stage,    c->status_d,   c->dbg_pairs, c->dbg_hsum,
-                    c->dbg_hxor,  c->dbg_cand, c->dbg_acc,  c->dbg_cell};
+                    c->dbg_hxor,  c->dbg_cand, c->dbg_acc,  c->dbg_cell, c->edit_flag, c->edit_off,
+                    c->edit_scan, c->edit_cnt};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (c->status_h) cudaFreeHost(c->status_h);
@@ -632,6 +641,7 @@ int plg_upload(plg_ctx* c, int64_t n, const double* pos, const double* vel, cons
     if (rc) return rc;
     if (c->n != n) c->graph_dirty = true;
     c->n = n;
+    c->next_id = n;
     c->fp.n = (int)n;
     c->bins_dirty = false;
     c->state_valid = true;
@@ -711,6 +721,253 @@ int plg_download(plg_ctx* c, double* pos, double* vel, int32_t* type, int32_t* i
     }
     CK(c, cudaStreamSynchronize(st));
     return PLG_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+// Scratch of the device-side edits, sized to the capacity.
+int edit_scratch(plg_ctx* c) {
+    if (c->edit_flag) return PLG_OK;
+    const size_t cap = (size_t)c->cap;
+    const int blocks = scan_blocks((int)std::max<int64_t>(c->cap, 1));
+    auto dm = [&](void** p, size_t bytes) -> int {
+        cudaError_t e = cudaMalloc(p, bytes);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            *p = nullptr;
+            return set_err(c, PLG_E_NO_MEMORY, "cudaMalloc (edit scratch)");
+        }
+        return PLG_OK;
+    };
+    int rc;
+    if ((rc = dm((void**)&c->edit_flag, sizeof(uint32_t) * (cap + 4)))) return rc;
+    if ((rc = dm((void**)&c->edit_off, sizeof(uint32_t) * (cap + 4)))) return rc;
+    if ((rc = dm((void**)&c->edit_scan, sizeof(unsigned long long) * (size_t)(blocks + 1)))) return rc;
+    if ((rc = dm((void**)&c->edit_cnt, sizeof(unsigned long long)))) return rc;
+    c->edit_scan_cap = blocks + 1;
+    return PLG_OK;
+}
+
+CursorDev cursor_dev(const plg_ctx* c, const plg_cursor* k) {
+    CursorDev cu;
+    cu.x = k->x;
+    cu.y = k->y;
+    cu.z = k->z;
+    cu.size = k->size;
+    cu.shape = k->shape;
+    cu.wrap = c->s.wrap ? 1 : 0;
+    return cu;
+}
+
+int check_cursor(plg_ctx* c, const plg_cursor* k) {
+    if (!k) return set_err(c, PLG_E_INVALID_ARG, "NULL cursor");
+    if (k->shape < PLG_CURSOR_CIRCLE || k->shape > PLG_CURSOR_INFINITY)
+        return set_err(c, PLG_E_INVALID_ARG, "unknown cursor shape");
+    if (!std::isfinite(k->x) || !std::isfinite(k->y) || !std::isfinite(k->z) || !(k->size >= 0) ||
+        !std::isfinite(k->size))
+        return set_err(c, PLG_E_INVALID_ARG, "cursor position and size must be finite, size >= 0");
+    return PLG_OK;
+}
+
+// Marks the particles inside the cursor (edit_flag) and returns how many.
+int mark_cursor(plg_ctx* c, const plg_cursor* k, int64_t* count) {
+    int rc = edit_scratch(c);
+    if (rc) return rc;
+    cudaStream_t st = c->stream;
+    CK(c, cudaMemsetAsync(c->edit_cnt, 0, sizeof(unsigned long long), st));
+    const CursorDev cu = cursor_dev(c, k);
+    if (c->dim == 2)
+        launch_cursor_mark<2>(st, (int)c->n, c->apt, cu, c->edit_flag, c->edit_cnt);
+    else
+        launch_cursor_mark<3>(st, (int)c->n, c->apt, cu, c->edit_flag, c->edit_cnt);
+    CK(c, cudaGetLastError());
+    unsigned long long h = 0;
+    CK(c, cudaMemcpyAsync(&h, c->edit_cnt, sizeof(h), cudaMemcpyDeviceToHost, st));
+    CK(c, cudaStreamSynchronize(st));
+    *count = (int64_t)h;
+    return PLG_OK;
+}
+
+// After an edit of A: the next step re-bins, and a new particle count or
+// swapped buffers mean a new step graph.
+void edited(plg_ctx* c, int64_t n) {
+    if (n != c->n) c->graph_dirty = true;
+    c->n = n;
+    c->fp.n = (int)n;
+    c->bins_dirty = true;
+}
+
+void swap_ab(plg_ctx* c) {
+    std::swap(c->apt, c->bpt);
+    std::swap(c->avel, c->bvel);
+    c->graph_dirty = true;
+}
+
+}  // namespace
+
+extern "C" {
+
+int plg_cursor_count(plg_ctx* c, const plg_cursor* k, int64_t* count) {
+    int rc = check_ready(c);
+    if (rc) return rc;
+    if ((rc = check_cursor(c, k))) return rc;
+    if (!count) return set_err(c, PLG_E_INVALID_ARG, "NULL count");
+    DeviceGuard g(c->device);
+    CK(c, cudaStreamSynchronize(c->stream));
+    return mark_cursor(c, k, count);
+}
+
+int plg_cursor_move(plg_ctx* c, const plg_cursor* k, double dx, double dy, double dz, int64_t* moved) {
+    int rc = check_ready(c);
+    if (rc) return rc;
+    if ((rc = check_cursor(c, k))) return rc;
+    if (!std::isfinite(dx) || !std::isfinite(dy) || !std::isfinite(dz))
+        return set_err(c, PLG_E_INVALID_ARG, "displacement must be finite");
+    DeviceGuard g(c->device);
+    CK(c, cudaStreamSynchronize(c->stream));
+    int64_t cnt = 0;
+    if ((rc = mark_cursor(c, k, &cnt))) return rc;
+    if (moved) *moved = cnt;
+    if (cnt == 0) return PLG_OK;
+    if (c->dim == 2)
+        launch_cursor_move<2>(c->stream, (int)c->n, c->apt, c->edit_flag, dx, dy, c->dim == 3 ? dz : 0.0,
+                              c->s.wrap ? 1 : 0);
+    else
+        launch_cursor_move<3>(c->stream, (int)c->n, c->apt, c->edit_flag, dx, dy, dz, c->s.wrap ? 1 : 0);
+    CK(c, cudaGetLastError());
+    CK(c, cudaStreamSynchronize(c->stream));
+    edited(c, c->n);
+    return PLG_OK;
+}
+
+int plg_cursor_delete(plg_ctx* c, const plg_cursor* k, int64_t* deleted) {
+    int rc = check_ready(c);
+    if (rc) return rc;
+    if ((rc = check_cursor(c, k))) return rc;
+    DeviceGuard g(c->device);
+    CK(c, cudaStreamSynchronize(c->stream));
+    int64_t cnt = 0;
+    if ((rc = mark_cursor(c, k, &cnt))) return rc;
+    if (deleted) *deleted = cnt;
+    if (cnt == 0) return PLG_OK;
+    cudaStream_t st = c->stream;
+    const int n = (int)c->n;
+    launch_invert(st, n, c->edit_flag);  // 1 = keep
+    CK(c, cudaMemsetAsync(c->edit_scan, 0, sizeof(unsigned long long) * (size_t)(scan_blocks(n) + 1), st));
+    launch_scan(st, c->edit_flag, n, c->edit_off, c->edit_scan, c->status_d, nullptr);
+    if (c->dim == 2)
+        launch_compact<2>(st, n, c->edit_off, buf_a<2>(c), buf_b<2>(c));
+    else
+        launch_compact<3>(st, n, c->edit_off, buf_a<3>(c), buf_b<3>(c));
+    CK(c, cudaGetLastError());
+    if ((rc = read_status(c))) return rc;
+    swap_ab(c);
+    edited(c, c->n - cnt);
+    return PLG_OK;
+}
+
+int plg_append(plg_ctx* c, int64_t n, const double* pos, const double* vel, const int32_t* type) {
+    int rc = check_ready(c);
+    if (rc) return rc;
+    if (n < 0) return set_err(c, PLG_E_INVALID_ARG, "negative particle count");
+    if (n == 0) return PLG_OK;
+    if (!pos || !type) return set_err(c, PLG_E_INVALID_ARG, "pos and type must not be NULL");
+    if (c->n + n > c->cap) return set_err(c, PLG_E_CAPACITY, "more particles than the context capacity");
+    if (c->next_id + n > INT32_MAX) return set_err(c, PLG_E_CAPACITY, "particle ids exhausted");
+    DeviceGuard g(c->device);
+    cudaStream_t st = c->stream;
+    CK(c, cudaStreamSynchronize(st));
+    double* dpos = (double*)c->stage;
+    double* dvel = dpos + 3 * stage_rows(c->cap);
+    int32_t* dtype = (int32_t*)(dvel + 3 * stage_rows(c->cap));
+    const double* mpos = host_mapped(pos);
+    const double* mvel = host_mapped(vel);
+    const int32_t* mtype = host_mapped(type);
+    if (mpos)
+        dpos = const_cast<double*>(mpos);
+    else
+        CK(c, cudaMemcpyAsync(dpos, pos, sizeof(double) * 3 * (size_t)n, cudaMemcpyHostToDevice, st));
+    if (mvel)
+        dvel = const_cast<double*>(mvel);
+    else if (vel)
+        CK(c, cudaMemcpyAsync(dvel, vel, sizeof(double) * 3 * (size_t)n, cudaMemcpyHostToDevice, st));
+    if (mtype)
+        dtype = const_cast<int32_t*>(mtype);
+    else
+        CK(c, cudaMemcpyAsync(dtype, type, sizeof(int32_t) * (size_t)n, cudaMemcpyHostToDevice, st));
+    CK(c, cudaMemsetAsync(c->status_d, 0, sizeof(uint32_t), st));
+    const int64_t off = c->n;
+    if (c->dim == 2)
+        launch_upload<2>(st, (int)n, dpos, vel ? dvel : nullptr, dtype, c->ntypes,
+                         StateBuf<2>{c->apt + off, (float2*)c->avel + off}, c->cell + off, c->rank + off, c->counts,
+                         grid_of(c), c->status_d, 0, (int)c->next_id);
+    else
+        launch_upload<3>(st, (int)n, dpos, vel ? dvel : nullptr, dtype, c->ntypes,
+                         StateBuf<3>{c->apt + off, (float4*)c->avel + off}, c->cell + off, c->rank + off, c->counts,
+                         grid_of(c), c->status_d, 0, (int)c->next_id);
+    CK(c, cudaGetLastError());
+    if ((rc = read_status(c))) return rc;
+    c->next_id += n;
+    edited(c, c->n + n);
+    return PLG_OK;
+}
+
+int plg_permute(plg_ctx* c, int64_t n_new, const int32_t* src) {
+    int rc = check_ready(c);
+    if (rc) return rc;
+    if (n_new < 0 || n_new > c->cap) return set_err(c, PLG_E_INVALID_ARG, "bad particle count");
+    if (n_new > 0 && !src) return set_err(c, PLG_E_INVALID_ARG, "NULL index array");
+    {
+        // Distinct indices of the current order: checked before anything changes.
+        std::vector<char> seen((size_t)c->n, 0);
+        for (int64_t k = 0; k < n_new; ++k) {
+            const int32_t j = src[k];
+            if (j < 0 || j >= c->n) return set_err(c, PLG_E_INVALID_ARG, "index outside the particles");
+            if (seen[(size_t)j]) return set_err(c, PLG_E_INVALID_ARG, "repeated index");
+            seen[(size_t)j] = 1;
+        }
+    }
+    DeviceGuard g(c->device);
+    if ((rc = edit_scratch(c))) return rc;
+    cudaStream_t st = c->stream;
+    CK(c, cudaStreamSynchronize(st));
+    CK(c, cudaMemsetAsync(c->status_d, 0, sizeof(uint32_t), st));
+    if (n_new > 0)
+        CK(c, cudaMemcpyAsync(c->edit_flag, src, sizeof(int32_t) * (size_t)n_new, cudaMemcpyHostToDevice, st));
+    if (c->dim == 2)
+        launch_permute<2>(st, (int)n_new, (const int32_t*)c->edit_flag, (int)c->n, buf_a<2>(c), buf_b<2>(c),
+                          c->status_d);
+    else
+        launch_permute<3>(st, (int)n_new, (const int32_t*)c->edit_flag, (int)c->n, buf_a<3>(c), buf_b<3>(c),
+                          c->status_d);
+    CK(c, cudaGetLastError());
+    if ((rc = read_status(c))) return rc;  // a bad index leaves A untouched
+    swap_ab(c);
+    edited(c, n_new);
+    return PLG_OK;
+}
+
+int plg_set_types(plg_ctx* c, const int32_t* type) {
+    int rc = check_ready(c);
+    if (rc) return rc;
+    if (!type) return set_err(c, PLG_E_INVALID_ARG, "NULL type array");
+    for (int64_t i = 0; i < c->n; ++i)
+        if (type[i] < 0 || type[i] >= c->ntypes) return set_err(c, PLG_E_INVALID_ARG, "type outside [0, matrix size)");
+    DeviceGuard g(c->device);
+    if ((rc = edit_scratch(c))) return rc;
+    cudaStream_t st = c->stream;
+    CK(c, cudaStreamSynchronize(st));
+    CK(c, cudaMemsetAsync(c->status_d, 0, sizeof(uint32_t), st));
+    if (c->n > 0)
+        CK(c, cudaMemcpyAsync(c->edit_flag, type, sizeof(int32_t) * (size_t)c->n, cudaMemcpyHostToDevice, st));
+    if (c->dim == 2)
+        launch_set_types<2>(st, (int)c->n, (const int32_t*)c->edit_flag, c->ntypes, c->apt, c->status_d);
+    else
+        launch_set_types<3>(st, (int)c->n, (const int32_t*)c->edit_flag, c->ntypes, c->apt, c->status_d);
+    CK(c, cudaGetLastError());
+    return read_status(c);
 }
 
 int plg_particle_count(plg_ctx* c, int64_t* n) {

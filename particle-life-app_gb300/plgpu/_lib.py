@@ -56,6 +56,16 @@ class plg_world_desc(C.Structure):
     ]
 
 
+class plg_cursor(C.Structure):
+    _fields_ = [("x", C.c_double), ("y", C.c_double), ("z", C.c_double), ("size", C.c_double),
+                ("shape", C.c_int32), ("reserved", C.c_int32)]
+
+
+PLG_CURSOR_CIRCLE = 0
+PLG_CURSOR_SQUARE = 1
+PLG_CURSOR_INFINITY = 2
+
+
 class plg_server_config(C.Structure):
     _fields_ = [
         ("memory_budget_bytes", C.c_int64),
@@ -151,6 +161,12 @@ SIGNATURES = {
     "plg_batch_autotune": (C.c_int, [_P, C.c_int32, _I32P, _DP]),
     "plg_batch_set_steps": (C.c_int, [_P, C.c_int32, C.c_int32]),
     "plg_batch_steps_left": (C.c_int, [_P, C.c_int32, _I32P]),
+    "plg_cursor_count": (C.c_int, [_P, C.POINTER(plg_cursor), _I64P]),
+    "plg_cursor_move": (C.c_int, [_P, C.POINTER(plg_cursor), C.c_double, C.c_double, C.c_double, _I64P]),
+    "plg_cursor_delete": (C.c_int, [_P, C.POINTER(plg_cursor), _I64P]),
+    "plg_append": (C.c_int, [_P, C.c_int64, _DP, _DP, _I32P]),
+    "plg_permute": (C.c_int, [_P, C.c_int64, _I32P]),
+    "plg_set_types": (C.c_int, [_P, _I32P]),
     "plg_world_check": (C.c_int, [C.c_int32, C.POINTER(plg_world_desc)]),
     "plg_world_device_bytes": (C.c_int64, [C.c_int32, C.POINTER(plg_world_desc)]),
     "plg_server_create": (C.c_int, [C.POINTER(plg_server_config), C.POINTER(_P)]),

@@ -319,6 +319,47 @@ class GpuWorld:
         self._c(self.lib.plg_step_stats(self.ctx, _lib.C.byref(v)), "plg_step_stats")
         return v.value
 
+    # -- edits on the device (no re-upload) --
+
+    def _cursor(self, x, y, z, size, shape):
+        return _lib.plg_cursor(float(x), float(y), float(z), float(size), int(shape), 0)
+
+    def cursor_count(self, x, y, z=0.0, size=0.1, shape=_lib.PLG_CURSOR_CIRCLE) -> int:
+        v = _lib.C.c_int64()
+        k = self._cursor(x, y, z, size, shape)
+        self._c(self.lib.plg_cursor_count(self.ctx, _lib.C.byref(k), _lib.C.byref(v)), "plg_cursor_count")
+        return v.value
+
+    def cursor_move(self, x, y, z, size, shape, dx, dy, dz=0.0) -> int:
+        v = _lib.C.c_int64()
+        k = self._cursor(x, y, z, size, shape)
+        self._c(self.lib.plg_cursor_move(self.ctx, _lib.C.byref(k), dx, dy, dz, _lib.C.byref(v)), "plg_cursor_move")
+        return v.value
+
+    def cursor_delete(self, x, y, z=0.0, size=0.1, shape=_lib.PLG_CURSOR_CIRCLE) -> int:
+        v = _lib.C.c_int64()
+        k = self._cursor(x, y, z, size, shape)
+        self._c(self.lib.plg_cursor_delete(self.ctx, _lib.C.byref(k), _lib.C.byref(v)), "plg_cursor_delete")
+        return v.value
+
+    def append(self, pos: np.ndarray, vel: Optional[np.ndarray], types: np.ndarray) -> None:
+        pos = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1, 3)
+        velp = None
+        if vel is not None:
+            vel = np.ascontiguousarray(vel, dtype=np.float64).reshape(-1, 3)
+            velp = _lib.ptr(vel, _lib.C.c_double)
+        types = np.ascontiguousarray(types, dtype=np.int32)
+        self._c(self.lib.plg_append(self.ctx, pos.shape[0], _lib.ptr(pos, _lib.C.c_double), velp,
+                                    _lib.ptr(types, _lib.C.c_int32)), "plg_append")
+
+    def permute(self, src: np.ndarray) -> None:
+        src = np.ascontiguousarray(src, dtype=np.int32)
+        self._c(self.lib.plg_permute(self.ctx, src.shape[0], _lib.ptr(src, _lib.C.c_int32)), "plg_permute")
+
+    def set_types(self, types: np.ndarray) -> None:
+        types = np.ascontiguousarray(types, dtype=np.int32)
+        self._c(self.lib.plg_set_types(self.ctx, _lib.ptr(types, _lib.C.c_int32)), "plg_set_types")
+
     def request_stop(self) -> None:
         self._c(self.lib.plg_request_stop(self.ctx), "plg_request_stop")
 

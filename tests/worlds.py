@@ -97,10 +97,11 @@ def run_gpu_debug(spec: WorldSpec, capacity=None):
     return d, st
 
 
-def run_oracle_debug(spec: WorldSpec, threads=8):
+def run_oracle_debug(spec: WorldSpec, threads=8, ids=None):
     import orc
 
-    o = orc.World(spec.dim, spec.pos, spec.vel, spec.types, np.arange(spec.n, dtype=np.int32), spec.matrix,
+    ids = np.arange(spec.n, dtype=np.int32) if ids is None else np.ascontiguousarray(ids, np.int32)
+    o = orc.World(spec.dim, spec.pos, spec.vel, spec.types, ids, spec.matrix,
                   orc.settings(spec.rmax, spec.friction, spec.force, spec.dt, spec.beta, spec.wrap))
     d = o.step(threads=threads, debug=True)
     return d, o
@@ -123,11 +124,12 @@ VEL_TOL = 1e-5
 POS_ABS = 1.2e-7
 
 
-def compare_with_oracle(spec: WorldSpec, g: dict, state, exact_only=False, normwise=True):
+def compare_with_oracle(spec: WorldSpec, g: dict, state, exact_only=False, normwise=True, ids=None):
     """Asserts one GPU step (debug outputs `g`, downloaded `state`) against
-    the oracle's step of the same start state; returns error figures."""
+    the oracle's step of the same start state (particle ids `ids`, default
+    0..n-1); returns error figures."""
     gpos, gvel, gtypes, gids = state
-    d, o = run_oracle_debug(spec)
+    d, o = run_oracle_debug(spec, ids=ids)
     assert np.array_equal(gids, o.ids), "sorted order (ids) differs from the oracle"
     assert np.array_equal(gtypes, o.types)
     assert np.array_equal(g["cell"], d["cell"]), "cell assignment differs"
@@ -153,3 +155,29 @@ def compare_with_oracle(spec: WorldSpec, g: dict, state, exact_only=False, normw
     assert np.all(dp <= bound), float((dp / bound).max())
     out.update(e)
     return out
+
+
+def cursor_inside(pos: np.ndarray, x, y, z, size, shape, wrap: bool) -> np.ndarray:
+    """Cursor.isInside (app/cursors/Cursor.java:16-35) in FP64: delta to the
+    cursor, wrapped as val - floor(val + 0.5), divided by the size, then the
+    shape's test (0 circle: length <= 0.5, 1 square: |x|, |y| <= 0.5,
+    2 infinity)."""
+    if size == 0.0:
+        return np.zeros(pos.shape[0], bool)
+    d = np.asarray(pos, np.float64) - np.array([x, y, z], np.float64)
+    if wrap:
+        d = d - np.floor(d + 0.5)
+    d = d / size
+    if shape == 0:
+        return np.sqrt(d[:, 0] * d[:, 0] + (d[:, 1] * d[:, 1] + d[:, 2] * d[:, 2])) <= 0.5
+    if shape == 1:
+        return (np.abs(d[:, 0]) <= 0.5) & (np.abs(d[:, 1]) <= 0.5)
+    return np.ones(pos.shape[0], bool)
+
+
+def ensure_position_f64(x: np.ndarray, wrap: bool) -> np.ndarray:
+    """Range.wrap / Range.clamp (backend/Range.java:40-96) of FP64 values."""
+    if wrap:
+        x = x - np.floor(x)
+        return np.where(x >= 1.0, 0.0, x)
+    return np.clip(x, 0.0, 1.0)
