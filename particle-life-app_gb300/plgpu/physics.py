@@ -610,6 +610,44 @@ class Physics:
         """Brings the host arrays up to date (for sync_policy='manual')."""
         self._sync_host()
 
+    # -- saves (app/Main.java:1258-1348) --
+
+    def save_state(self, path, image_png: Optional[bytes] = None) -> None:
+        """Main.saveState: particles, settings and matrix in the app's zip layout."""
+        from . import saves
+
+        self._sync_host()
+        s = self.settings
+        saves.save_state(path, self.positions, self.velocities, self.types, wrap=s.wrap, rmax=s.rmax,
+                         friction=s.friction, force=s.force, matrix=matrix_to_array(s.matrix), dim=self.dim,
+                         image_png=image_png)
+
+    def load_state(self, path) -> None:
+        """Main.loadState: each entry present replaces that part of the state;
+        a new matrix re-types particles outside it (ensureTypes)."""
+        from . import saves
+
+        st = saves.load_state(path)
+        self._sync_host()
+        if st.positions is not None:
+            self.positions = st.positions.copy()
+            self.velocities = st.velocities.copy()
+            self.types = st.types.astype(np.int32)
+            self.ids = np.arange(len(self.types), dtype=np.int32)
+            for i in range(len(self.types)):
+                self.ensure_position(self.positions[i])
+        if st.rmax is not None:
+            self.settings.wrap, self.settings.rmax = st.wrap, st.rmax
+            self.settings.friction, self.settings.force = st.friction, st.force
+        if st.matrix is not None:
+            m = DefaultMatrix(st.matrix.shape[0])
+            for i in range(st.matrix.shape[0]):
+                for j in range(st.matrix.shape[0]):
+                    m.set(i, j, float(st.matrix[i, j]))
+            self.settings.matrix = m
+            self.ensure_types()
+        self._host_dirty = True
+
     def close(self) -> None:
         if self._world is not None:
             self._world.close()
