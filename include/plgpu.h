@@ -141,6 +141,56 @@ int plg_download(plg_ctx* ctx, double* pos, double* vel, int32_t* type,
 
 int plg_particle_count(plg_ctx* ctx, int64_t* n);
 
+/* ---- initialisers on the device ------------------------------------------ */
+
+/* The app's catalogues as seeded generators (Philox4x64-10 per particle:
+ * key (seed, 0), counter (index, stream, 0, 0)).  Position setters of
+ * app/PositionSetterProvider.java:16-119 (UNIFORM is
+ * backend/DefaultPositionSetter.java); type setters of
+ * app/TypeSetterProvider.java:11-45 (RANDOM is DefaultTypeSetter); matrix
+ * generators of app/MatrixGeneratorProvider.java:13-79 (RANDOM is
+ * DefaultMatrix.randomize).  3D worlds get a third coordinate (uniform; normal
+ * for CENTERED): an extension, the app is 2D. */
+#define PLG_POS_UNIFORM 0
+#define PLG_POS_CENTERED 1
+#define PLG_POS_UNIFORM_CIRCLE 2
+#define PLG_POS_CENTERED_CIRCLE 3
+#define PLG_POS_RING 4
+#define PLG_POS_RAINBOW_RING 5
+#define PLG_POS_COLOR_BATTLE 6
+#define PLG_POS_COLOR_WHEEL 7
+#define PLG_POS_LINE 8
+#define PLG_POS_SPIRAL 9
+#define PLG_POS_RAINBOW_SPIRAL 10
+#define PLG_TYPE_RANDOM 0
+#define PLG_TYPE_RANDOMIZE_10 1
+#define PLG_TYPE_SLICES 2
+#define PLG_TYPE_ONION 3
+#define PLG_TYPE_ROTATE 4
+#define PLG_TYPE_FLIP 5
+#define PLG_TYPE_MORE_OF_FIRST 6
+#define PLG_TYPE_KILL_STILL 7
+#define PLG_MATRIX_RANDOM 0
+#define PLG_MATRIX_SYMMETRY 1
+#define PLG_MATRIX_CHAINS 2
+#define PLG_MATRIX_CHAINS_2 3
+#define PLG_MATRIX_CHAINS_3 4
+#define PLG_MATRIX_SNAKES 5
+#define PLG_MATRIX_ZERO 6
+
+/* Replaces the particles with n new ones made on the device the way
+ * Physics.setParticleCount makes them from nothing (Physics.java:190-196,
+ * 285-295): type from the type setter, then position from the position
+ * setter, ensurePosition, velocity 0; ids 0..n-1. */
+int plg_generate(plg_ctx* ctx, int64_t n, int32_t position_setter, int32_t type_setter,
+                 uint64_t seed);
+/* Physics.setPositions (Physics.java:166-168) with a catalogue setter. */
+int plg_apply_position_setter(plg_ctx* ctx, int32_t setter, uint64_t seed);
+/* Physics.setTypes (Physics.java:509-511) with a catalogue type setter. */
+int plg_apply_type_setter(plg_ctx* ctx, int32_t setter, uint64_t seed);
+/* A catalogue matrix, row-major size x size doubles.  Host only. */
+int plg_generate_matrix(int32_t generator, int32_t size, uint64_t seed, double* out);
+
 /* ---- edits on the device (no re-upload) --------------------------------- */
 
 /* A cursor of app/cursors/Cursor.java:10-13: position, size and shape

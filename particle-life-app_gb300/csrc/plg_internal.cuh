@@ -172,6 +172,32 @@ void launch_upload(cudaStream_t st, int n, const double* pos, const double* vel,
                    int ntypes, StateBuf<D> a, uint32_t* cell, uint32_t* rank, uint32_t* counts, Grid g,
                    uint32_t* status, uint32_t cell_base = 0, int id_base = 0);
 
+// ---- initialisers (k_init.cu) ----
+// Position setters (app/PositionSetterProvider.java), type setters
+// (app/TypeSetterProvider.java) and matrix generators
+// (app/MatrixGeneratorProvider.java), numbered as in include/plgpu.h.
+enum PositionSetterKind {
+    kPosUniform = 0, kPosCentered, kPosUniformCircle, kPosCenteredCircle, kPosRing, kPosRainbowRing,
+    kPosColorBattle, kPosColorWheel, kPosLine, kPosSpiral, kPosRainbowSpiral, kPosCount
+};
+enum TypeSetterKind {
+    kTypeRandom = 0, kTypeRandomize10, kTypeSlices, kTypeOnion, kTypeRotate, kTypeFlip, kTypeMoreOfFirst,
+    kTypeKillStill, kTypeCount
+};
+enum MatrixGeneratorKind {
+    kMatrixRandom = 0, kMatrixSymmetry, kMatrixChains, kMatrixChains2, kMatrixChains3, kMatrixSnakes, kMatrixZero,
+    kMatrixCount
+};
+template <int D>
+void launch_generate(cudaStream_t st, int n, int pos_setter, int type_setter, unsigned long long seed, int ntypes,
+                     int wrap, StateBuf<D> a);
+template <int D>
+void launch_apply_positions(cudaStream_t st, int n, int setter, unsigned long long seed, int ntypes, int wrap,
+                            StateBuf<D> a);
+template <int D>
+void launch_apply_types(cudaStream_t st, int n, int setter, unsigned long long seed, int ntypes, StateBuf<D> a);
+void generate_matrix(int kind, int size, unsigned long long seed, double* m);
+
 // ---- device-side edits (k_edit.cu) ----
 // flag[i] = particle i inside the cursor; *count += the number inside.
 template <int D>

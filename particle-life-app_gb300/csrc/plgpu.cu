@@ -970,6 +970,69 @@ int plg_set_types(plg_ctx* c, const int32_t* type) {
     return read_status(c);
 }
 
+int plg_generate(plg_ctx* c, int64_t n, int32_t position_setter, int32_t type_setter, uint64_t seed) {
+    if (!c) return PLG_E_INVALID_ARG;
+    if (n < 0) return set_err(c, PLG_E_INVALID_ARG, "negative particle count");
+    if (n > c->cap) return set_err(c, PLG_E_CAPACITY, "more particles than the context capacity");
+    if (position_setter < 0 || position_setter >= kPosCount || type_setter < 0 || type_setter >= kTypeCount)
+        return set_err(c, PLG_E_INVALID_ARG, "unknown setter");
+    if (!c->have_settings) return set_err(c, PLG_E_STATE, "plg_set_settings has not been called");
+    if (!c->have_matrix) return set_err(c, PLG_E_STATE, "plg_set_matrix has not been called");
+    DeviceGuard g(c->device);
+    cudaStream_t st = c->stream;
+    CK(c, cudaStreamSynchronize(st));
+    if (c->dim == 2)
+        launch_generate<2>(st, (int)n, position_setter, type_setter, seed, c->ntypes, c->s.wrap ? 1 : 0, buf_a<2>(c));
+    else
+        launch_generate<3>(st, (int)n, position_setter, type_setter, seed, c->ntypes, c->s.wrap ? 1 : 0, buf_a<3>(c));
+    CK(c, cudaGetLastError());
+    CK(c, cudaStreamSynchronize(st));
+    if (c->n != n) c->graph_dirty = true;
+    c->n = n;
+    c->next_id = n;
+    c->fp.n = (int)n;
+    c->bins_dirty = true;
+    c->state_valid = true;
+    return PLG_OK;
+}
+
+int plg_apply_position_setter(plg_ctx* c, int32_t setter, uint64_t seed) {
+    int rc = check_ready(c);
+    if (rc) return rc;
+    if (setter < 0 || setter >= kPosCount) return set_err(c, PLG_E_INVALID_ARG, "unknown position setter");
+    DeviceGuard g(c->device);
+    cudaStream_t st = c->stream;
+    if (c->dim == 2)
+        launch_apply_positions<2>(st, (int)c->n, setter, seed, c->ntypes, c->s.wrap ? 1 : 0, buf_a<2>(c));
+    else
+        launch_apply_positions<3>(st, (int)c->n, setter, seed, c->ntypes, c->s.wrap ? 1 : 0, buf_a<3>(c));
+    CK(c, cudaGetLastError());
+    CK(c, cudaStreamSynchronize(st));
+    c->bins_dirty = true;
+    return PLG_OK;
+}
+
+int plg_apply_type_setter(plg_ctx* c, int32_t setter, uint64_t seed) {
+    int rc = check_ready(c);
+    if (rc) return rc;
+    if (setter < 0 || setter >= kTypeCount) return set_err(c, PLG_E_INVALID_ARG, "unknown type setter");
+    DeviceGuard g(c->device);
+    cudaStream_t st = c->stream;
+    if (c->dim == 2)
+        launch_apply_types<2>(st, (int)c->n, setter, seed, c->ntypes, buf_a<2>(c));
+    else
+        launch_apply_types<3>(st, (int)c->n, setter, seed, c->ntypes, buf_a<3>(c));
+    CK(c, cudaGetLastError());
+    CK(c, cudaStreamSynchronize(st));
+    return PLG_OK;
+}
+
+int plg_generate_matrix(int32_t generator, int32_t size, uint64_t seed, double* out) {
+    if (generator < 0 || generator >= kMatrixCount || size < 1 || size > kMaxTypes || !out) return PLG_E_INVALID_ARG;
+    generate_matrix(generator, size, seed, out);
+    return PLG_OK;
+}
+
 int plg_particle_count(plg_ctx* c, int64_t* n) {
     if (!c || !n) return PLG_E_INVALID_ARG;
     *n = c->n;

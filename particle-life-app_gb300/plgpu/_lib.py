@@ -61,6 +61,11 @@ class plg_cursor(C.Structure):
                 ("shape", C.c_int32), ("reserved", C.c_int32)]
 
 
+POSITION_SETTERS = ["uniform", "centered", "uniform circle", "centered circle", "ring", "rainbow ring",
+                    "color battle", "color wheel", "line", "spiral", "rainbow spiral"]
+TYPE_SETTERS = ["random", "randomize 10%", "slices", "onion", "rotate", "flip", "more of first", "kill still"]
+MATRIX_GENERATORS = ["random", "symmetry", "chains", "chains 2", "chains 3", "snakes", "zero"]
+
 PLG_CURSOR_CIRCLE = 0
 PLG_CURSOR_SQUARE = 1
 PLG_CURSOR_INFINITY = 2
@@ -167,6 +172,10 @@ SIGNATURES = {
     "plg_append": (C.c_int, [_P, C.c_int64, _DP, _DP, _I32P]),
     "plg_permute": (C.c_int, [_P, C.c_int64, _I32P]),
     "plg_set_types": (C.c_int, [_P, _I32P]),
+    "plg_generate": (C.c_int, [_P, C.c_int64, C.c_int32, C.c_int32, C.c_uint64]),
+    "plg_apply_position_setter": (C.c_int, [_P, C.c_int32, C.c_uint64]),
+    "plg_apply_type_setter": (C.c_int, [_P, C.c_int32, C.c_uint64]),
+    "plg_generate_matrix": (C.c_int, [C.c_int32, C.c_int32, C.c_uint64, _DP]),
     "plg_world_check": (C.c_int, [C.c_int32, C.POINTER(plg_world_desc)]),
     "plg_world_device_bytes": (C.c_int64, [C.c_int32, C.POINTER(plg_world_desc)]),
     "plg_server_create": (C.c_int, [C.POINTER(plg_server_config), C.POINTER(_P)]),

@@ -360,6 +360,17 @@ class GpuWorld:
         types = np.ascontiguousarray(types, dtype=np.int32)
         self._c(self.lib.plg_set_types(self.ctx, _lib.ptr(types, _lib.C.c_int32)), "plg_set_types")
 
+    # -- initialisers on the device --
+
+    def generate(self, n: int, position_setter: int = 0, type_setter: int = 0, seed: int = 0) -> None:
+        self._c(self.lib.plg_generate(self.ctx, n, position_setter, type_setter, seed), "plg_generate")
+
+    def apply_position_setter(self, setter: int, seed: int = 0) -> None:
+        self._c(self.lib.plg_apply_position_setter(self.ctx, setter, seed), "plg_apply_position_setter")
+
+    def apply_type_setter(self, setter: int, seed: int = 0) -> None:
+        self._c(self.lib.plg_apply_type_setter(self.ctx, setter, seed), "plg_apply_type_setter")
+
     def request_stop(self) -> None:
         self._c(self.lib.plg_request_stop(self.ctx), "plg_request_stop")
 
