@@ -27,13 +27,32 @@ def check_step(spec: WorldSpec, gpu, exact_only=False, normwise=True):
     return compare_with_oracle(spec, g, state, exact_only=exact_only, normwise=normwise)
 
 
+def report(name, r):
+    print(f"\n{name}: interacting pairs/particle {r['pairs']:.2f}, acceleration error norm-wise "
+          f"{r.get('normwise', float('nan')):.2e}, per particle p99 {r.get('p99', float('nan')):.2e} "
+          f"max {r.get('max', float('nan')):.2e}")
+
+
 def test_cfg1_2d_10k(gpu):
-    check_step(uniform_world(10_000, 6, 0.02, seed=1, vel_scale=0.01, dt=0.02), gpu)
+    report("10k 2D", check_step(uniform_world(10_000, 6, 0.02, seed=1, vel_scale=0.01, dt=0.02), gpu))
 
 
 def test_cfg2_2d_1m(gpu):
     r = check_step(uniform_world(1_000_000, 8, 0.0025, seed=2, vel_scale=0.01, dt=0.01), gpu)
+    report("1M 2D", r)
     assert 18 < r["pairs"] < 21  # ~19.6 expected neighbours
+
+
+def test_cfg3_3d_4m_blobs(gpu):
+    """The 3D configuration at full size: 4M particles in 64 blobs, 16 types,
+    about 40 neighbours."""
+    from plgpu import workloads
+
+    w = workloads.blob_world_3d()
+    spec = WorldSpec(3, w.pos, np.zeros_like(w.pos), w.types, w.matrix, w.rmax, w.friction, w.force, w.dt)
+    r = check_step(spec, gpu)
+    report("4M 3D blobs", r)
+    assert 38 < r["pairs"] < 42
 
 
 def test_2d_clamp_with_walls(gpu):
