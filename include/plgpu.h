@@ -191,6 +191,31 @@ int plg_apply_type_setter(plg_ctx* ctx, int32_t setter, uint64_t seed);
 /* A catalogue matrix, row-major size x size doubles.  Host only. */
 int plg_generate_matrix(int32_t generator, int32_t size, uint64_t seed, double* out);
 
+/* ---- headless splat ------------------------------------------------------ */
+
+/* The app's default particle shaders (resources/shaders/default.vert, .geom,
+ * .frag) without a graphics API: each particle a disk of diameter `size`
+ * (world units) in its type's palette colour, with periodic copies across
+ * the edges when `wrap`; 16 samples per pixel, the last particle in the
+ * current order wins each sample (opaque "normal" blending), samples
+ * averaged.  Camera as NormalizedDeviceCoordinates: centre (cam_x, cam_y)
+ * and dimensions (cam_w, cam_h); top_left is the shader's camTopLeft.  The
+ * save thumbnail of app/Main.java:1143-1188 is centre (0.5, 0.5), dims
+ * (1, 1), top_left (0, 0), size 0.015, wrap 0. */
+typedef struct plg_render_params {
+    int32_t width, height;
+    double cam_x, cam_y, cam_w, cam_h;
+    double top_left_x, top_left_y;
+    double size;
+    int32_t wrap;
+    int32_t reserved;
+} plg_render_params;
+/* palette_rgba: ncolors x {r, g, b, a} floats in [0, 1] (types beyond the
+ * palette take its last colour); out_rgba: width x height x 4 bytes, rows
+ * bottom to top. */
+int plg_render(plg_ctx* ctx, const plg_render_params* params, int32_t ncolors,
+               const float* palette_rgba, uint8_t* out_rgba);
+
 /* ---- edits on the device (no re-upload) --------------------------------- */
 
 /* A cursor of app/cursors/Cursor.java:10-13: position, size and shape

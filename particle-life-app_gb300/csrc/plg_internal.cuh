@@ -198,6 +198,24 @@ template <int D>
 void launch_apply_types(cudaStream_t st, int n, int setter, unsigned long long seed, int ntypes, StateBuf<D> a);
 void generate_matrix(int kind, int size, unsigned long long seed, double* m);
 
+// ---- headless splat (k_splat.cu) ----
+// Camera as the app's NormalizedDeviceCoordinates (centre, dimensions, in
+// world units), camTopLeft and wrap as the default geometry shader's
+// uniforms, size = the particle diameter in world units.
+struct SplatParams {
+    int width, height;
+    float cam_x, cam_y, cam_w, cam_h;
+    float top_left_x, top_left_y;
+    float size;
+    int wrap;
+};
+int splat_samples_per_pixel();
+// winner: width * height * splat_samples_per_pixel() words of scratch;
+// palette: ncolors RGBA floats (device); out: width * height RGBA8 (device).
+template <int D>
+void launch_splat(cudaStream_t st, int n, const float4* pt, const SplatParams& S, uint32_t* winner,
+                  const float* palette, int ncolors, uint8_t* out);
+
 // ---- device-side edits (k_edit.cu) ----
 // flag[i] = particle i inside the cursor; *count += the number inside.
 template <int D>

@@ -1027,6 +1027,60 @@ int plg_apply_type_setter(plg_ctx* c, int32_t setter, uint64_t seed) {
     return PLG_OK;
 }
 
+int plg_render(plg_ctx* c, const plg_render_params* rp, int32_t ncolors, const float* palette_rgba,
+               uint8_t* out_rgba) {
+    int rc = check_ready(c);
+    if (rc) return rc;
+    if (!rp || !palette_rgba || !out_rgba || ncolors < 1) return set_err(c, PLG_E_INVALID_ARG, "NULL argument");
+    if (rp->width < 1 || rp->height < 1 || (int64_t)rp->width * rp->height > (1 << 26))
+        return set_err(c, PLG_E_INVALID_ARG, "image size must be 1..2^26 pixels");
+    if (!(rp->cam_w > 0) || !(rp->cam_h > 0) || !(rp->size >= 0) || !std::isfinite(rp->cam_x) ||
+        !std::isfinite(rp->cam_y) || !std::isfinite(rp->size))
+        return set_err(c, PLG_E_INVALID_ARG, "camera dimensions must be positive and finite");
+    DeviceGuard g(c->device);
+    cudaStream_t st = c->stream;
+    const size_t npix = (size_t)rp->width * rp->height;
+    uint32_t* winner = nullptr;
+    float* pal = nullptr;
+    uint8_t* img = nullptr;
+    auto release = [&] {
+        if (winner) cudaFree(winner);
+        if (pal) cudaFree(pal);
+        if (img) cudaFree(img);
+    };
+    if (cudaMalloc((void**)&winner, sizeof(uint32_t) * npix * splat_samples_per_pixel()) != cudaSuccess ||
+        cudaMalloc((void**)&pal, sizeof(float) * 4 * (size_t)ncolors) != cudaSuccess ||
+        cudaMalloc((void**)&img, 4 * npix) != cudaSuccess) {
+        cudaGetLastError();
+        release();
+        return set_err(c, PLG_E_NO_MEMORY, "cudaMalloc (render buffers)");
+    }
+    SplatParams S;
+    S.width = rp->width;
+    S.height = rp->height;
+    S.cam_x = (float)rp->cam_x;
+    S.cam_y = (float)rp->cam_y;
+    S.cam_w = (float)rp->cam_w;
+    S.cam_h = (float)rp->cam_h;
+    S.top_left_x = (float)rp->top_left_x;
+    S.top_left_y = (float)rp->top_left_y;
+    S.size = (float)rp->size;
+    S.wrap = rp->wrap ? 1 : 0;
+    cudaError_t e = cudaMemcpyAsync(pal, palette_rgba, sizeof(float) * 4 * (size_t)ncolors, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) {
+        if (c->dim == 2)
+            launch_splat<2>(st, (int)c->n, c->apt, S, winner, pal, ncolors, img);
+        else
+            launch_splat<3>(st, (int)c->n, c->apt, S, winner, pal, ncolors, img);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out_rgba, img, 4 * npix, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    release();
+    if (e != cudaSuccess) return cuda_fail(c, "plg_render", e);
+    return PLG_OK;
+}
+
 int plg_generate_matrix(int32_t generator, int32_t size, uint64_t seed, double* out) {
     if (generator < 0 || generator >= kMatrixCount || size < 1 || size > kMaxTypes || !out) return PLG_E_INVALID_ARG;
     generate_matrix(generator, size, seed, out);

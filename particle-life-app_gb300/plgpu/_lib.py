@@ -71,6 +71,12 @@ PLG_CURSOR_SQUARE = 1
 PLG_CURSOR_INFINITY = 2
 
 
+class plg_render_params(C.Structure):
+    _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("cam_x", C.c_double), ("cam_y", C.c_double),
+                ("cam_w", C.c_double), ("cam_h", C.c_double), ("top_left_x", C.c_double), ("top_left_y", C.c_double),
+                ("size", C.c_double), ("wrap", C.c_int32), ("reserved", C.c_int32)]
+
+
 class plg_server_config(C.Structure):
     _fields_ = [
         ("memory_budget_bytes", C.c_int64),
@@ -176,6 +182,7 @@ SIGNATURES = {
     "plg_apply_position_setter": (C.c_int, [_P, C.c_int32, C.c_uint64]),
     "plg_apply_type_setter": (C.c_int, [_P, C.c_int32, C.c_uint64]),
     "plg_generate_matrix": (C.c_int, [C.c_int32, C.c_int32, C.c_uint64, _DP]),
+    "plg_render": (C.c_int, [_P, C.POINTER(plg_render_params), C.c_int32, _FP, C.POINTER(C.c_uint8)]),
     "plg_world_check": (C.c_int, [C.c_int32, C.POINTER(plg_world_desc)]),
     "plg_world_device_bytes": (C.c_int64, [C.c_int32, C.POINTER(plg_world_desc)]),
     "plg_server_create": (C.c_int, [C.POINTER(plg_server_config), C.POINTER(_P)]),

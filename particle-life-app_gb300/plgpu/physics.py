@@ -371,6 +371,17 @@ class GpuWorld:
     def apply_type_setter(self, setter: int, seed: int = 0) -> None:
         self._c(self.lib.plg_apply_type_setter(self.ctx, setter, seed), "plg_apply_type_setter")
 
+    def render(self, width: int, height: int, palette: np.ndarray, cam=(0.5, 0.5, 1.0, 1.0), top_left=(0.0, 0.0),
+               size: float = 0.015, wrap: bool = False) -> np.ndarray:
+        """plg_render: (height, width, 4) uint8, rows bottom to top."""
+        pal = np.ascontiguousarray(palette, dtype=np.float32).reshape(-1, 4)
+        out = np.zeros((height, width, 4), np.uint8)
+        rp = _lib.plg_render_params(width, height, cam[0], cam[1], cam[2], cam[3], top_left[0], top_left[1], size,
+                                    1 if wrap else 0, 0)
+        self._c(self.lib.plg_render(self.ctx, _lib.C.byref(rp), pal.shape[0], _lib.ptr(pal, _lib.C.c_float),
+                                    out.ctypes.data_as(_lib.C.POINTER(_lib.C.c_uint8))), "plg_render")
+        return out
+
     def request_stop(self) -> None:
         self._c(self.lib.plg_request_stop(self.ctx), "plg_request_stop")
 
@@ -623,10 +634,24 @@ class Physics:
 
     # -- saves (app/Main.java:1258-1348) --
 
-    def save_state(self, path, image_png: Optional[bytes] = None) -> None:
-        """Main.saveState: particles, settings and matrix in the app's zip layout."""
+    def thumbnail(self, palette, size: int = 256) -> np.ndarray:
+        """Main.renderParticlesToImage (app/Main.java:1143-1188) on the GPU:
+        the whole world (camera centre (0.5, 0.5), dimensions (1, 1)),
+        particle size 0.015, no wrap, rows bottom to top.  `palette` holds
+        one RGBA colour per type (the app uses its natural-rainbow palette
+        sampled at the matrix size)."""
+        self._push()
+        return self.world.render(size, size, palette, cam=(0.5, 0.5, 1.0, 1.0), top_left=(0.0, 0.0), size=0.015,
+                                 wrap=False)
+
+    def save_state(self, path, image_png: Optional[bytes] = None, palette=None) -> None:
+        """Main.saveState: particles, settings and matrix in the app's zip
+        layout; with a palette (and no image given) the img.png thumbnail is
+        rendered on the GPU."""
         from . import saves
 
+        if image_png is None and palette is not None:
+            image_png = saves.png_rgba(self.thumbnail(palette, saves.THUMBNAIL_SIZE))
         self._sync_host()
         s = self.settings
         saves.save_state(path, self.positions, self.velocities, self.types, wrap=s.wrap, rmax=s.rmax,

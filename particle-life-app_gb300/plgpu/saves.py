@@ -21,8 +21,10 @@ from __future__ import annotations
 
 import io
 import math
+import struct
 import tomllib
 import zipfile
+import zlib
 from dataclasses import dataclass
 from typing import Optional
 
@@ -138,6 +140,45 @@ def parse_settings(text: str) -> dict:
     t = tomllib.loads(text)
     return {"wrap": t.get("boundaries", "periodic") == "periodic", "rmax": float(t.get("radius", 0.02)),
             "friction": float(t.get("friction", 0.85)), "force": float(t.get("force", 1.0))}
+
+
+THUMBNAIL_SIZE = 256  # Main.SAVE_IMAGE_SIZE (app/Main.java:168)
+
+
+def png_rgba(rows) -> bytes:
+    """An 8-bit RGBA PNG of a (height, width, 4) uint8 array; row 0 of the
+    array is the first row of the file.  The app stores glReadPixels rows
+    (bottom of the framebuffer first) unchanged (app/Main.java:1279-1289),
+    so plg_render's rows go in as they come."""
+    a = np.ascontiguousarray(rows, np.uint8)
+    h, w = a.shape[:2]
+
+    def chunk(kind: bytes, data: bytes) -> bytes:
+        return struct.pack(">I", len(data)) + kind + data + struct.pack(">I", zlib.crc32(kind + data) & 0xFFFFFFFF)
+
+    raw = b"".join(b"\x00" + a[j].tobytes() for j in range(h))  # filter type 0 per row
+    return (b"\x89PNG\r\n\x1a\n" + chunk(b"IHDR", struct.pack(">IIBBBBB", w, h, 8, 6, 0, 0, 0)) +
+            chunk(b"IDAT", zlib.compress(raw, 6)) + chunk(b"IEND", b""))
+
+
+def read_png_rgba(data: bytes) -> np.ndarray:
+    """Reads back what png_rgba writes (8-bit RGBA, filter type 0 rows)."""
+    assert data[:8] == b"\x89PNG\r\n\x1a\n"
+    off, idat, w, h = 8, b"", 0, 0
+    while off < len(data):
+        (ln,) = struct.unpack(">I", data[off:off + 4])
+        kind, body = data[off + 4:off + 8], data[off + 8:off + 8 + ln]
+        if kind == b"IHDR":
+            w, h, depth, ctype = struct.unpack(">IIBB", body[:10])
+            if depth != 8 or ctype != 6:
+                raise ValueError("only 8-bit RGBA")
+        elif kind == b"IDAT":
+            idat += body
+        off += 12 + ln
+    raw = np.frombuffer(zlib.decompress(idat), np.uint8).reshape(h, 1 + 4 * w)
+    if np.any(raw[:, 0] != 0):
+        raise ValueError("only filter type 0")
+    return raw[:, 1:].reshape(h, w, 4).copy()
 
 
 def save_state(path, positions, velocities, types, *, wrap: bool, rmax: float, friction: float, force: float,

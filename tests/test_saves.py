@@ -114,3 +114,13 @@ def test_a_loaded_save_continues_the_trajectory(gpu, tmp_path):
     assert np.array_equal(a.positions, b.positions) and np.array_equal(a.velocities, b.velocities)
     a.close()
     b.close()
+
+
+def test_png_round_trip():
+    """The thumbnail encoder writes an 8-bit RGBA PNG that reads back exactly."""
+    from plgpu import saves
+
+    img = np.random.default_rng(2).integers(0, 256, size=(37, 53, 4), dtype=np.uint8)
+    png = saves.png_rgba(img)
+    assert png[:8] == b"\x89PNG\r\n\x1a\n" and png[12:16] == b"IHDR"
+    assert np.array_equal(saves.read_png_rgba(png), img)
