@@ -59,7 +59,6 @@ struct plg_batch {
     void* avel = nullptr;
     void* bvel = nullptr;
     uint32_t* cell = nullptr;
-    uint32_t* rank = nullptr;
     uint32_t* perm = nullptr;
     uint32_t* slot_cell = nullptr;
     uint32_t* counts = nullptr;
@@ -180,7 +179,7 @@ void destroy_batch_graph(plg_batch* b) {
 
 void free_batch(plg_batch* b) {
     destroy_batch_graph(b);
-    void* ptrs[] = {b->apt,      b->bpt,       b->avel,      b->bvel,        b->cell,     b->rank,
+    void* ptrs[] = {b->apt,      b->bpt,       b->avel,      b->bvel,        b->cell,
                     b->perm,     b->slot_cell, b->counts,    b->cstart,      b->scan_state, b->defer,
                     b->status_d, b->worlds_d,  b->wp_off_d,  b->move_new_d,  b->move_old_d, b->bounds_d,
                     b->tile_off_d, b->steps_left_d,
@@ -390,7 +389,7 @@ int relayout(plg_batch* b, const std::vector<int>& survivors, const plg_world_de
         g.b_nx = w.bounds[w.nx];
         g.bounds = b->bounds_d + w.b_off;
         launch_upload<D>(st, (int)w.n, dpos, dvel, dtype, w.ntypes, sbuf<D>(b->bpt, b->bvel, w.p_off),
-                         b->cell + w.p_off, b->rank + w.p_off, b->counts, g, b->status_d, (uint32_t)w.c_off);
+                         b->cell + w.p_off, b->counts, g, b->status_d, (uint32_t)w.c_off);
         BCK(b, cudaGetLastError());
     }
     std::swap(b->apt, b->bpt);
@@ -398,7 +397,7 @@ int relayout(plg_batch* b, const std::vector<int>& survivors, const plg_world_de
     // Survivors: cells in the new global numbering and the next sort's counts.
     if (n_surv > 0) {
         launch_batch_rebin<D>(st, (int)n_surv, sbuf<D>(b->apt, b->avel, 0), b->worlds_d, b->wp_off_d,
-                              (int)survivors.size(), b->cell, b->rank, b->counts);
+                              (int)survivors.size(), b->cell, b->counts);
         BCK(b, cudaGetLastError());
     }
     BCK(b, cudaMemcpyAsync(b->status_h, b->status_d, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
@@ -415,12 +414,12 @@ void enqueue_batch_step(plg_batch* b, const DebugOut* dbg, int32_t* cell_sorted)
     const int nc = (int)std::max<int64_t>(b->c_total, 1);
     cudaMemsetAsync(b->scan_state, 0, sizeof(unsigned long long) * (size_t)(scan_blocks(nc) + 1), st);
     launch_scan(st, b->counts, nc, b->cstart, b->scan_state, b->status_d, b->defer);
-    launch_scatter(st, n, b->cell, b->rank, b->cstart, b->perm, b->slot_cell);
+    launch_scatter(st, n, b->cell, b->counts, b->cstart, b->perm, b->slot_cell);
     launch_gather<D>(st, n, b->perm, b->slot_cell, b->cstart, sbuf<D>(b->apt, b->avel, 0),
                      sbuf<D>(b->bpt, b->bvel, 0), cell_sorted);
     launch_force_batch<D>(st, b->worlds_d, b->wp_off_d, b->tile_off_d + (size_t)b->variant * (b->wcap + 1),
                           b->steps_left_d, b->tiles[b->variant], (int)b->worlds.size(), n, b->smem_matrix,
-                          sbuf<D>(b->bpt, b->bvel, 0), b->cstart, sbuf<D>(b->apt, b->avel, 0), b->cell, b->rank,
+                          sbuf<D>(b->bpt, b->bvel, 0), b->cstart, b->slot_cell, sbuf<D>(b->apt, b->avel, 0), b->cell,
                           b->counts, b->defer, dbg, b->variant);
     launch_batch_tick(st, b->steps_left_d, (int)b->worlds.size());
 }
@@ -492,7 +491,8 @@ int64_t plg_world_device_bytes(int32_t dim, const plg_world_desc* d) {
     if (!d || (dim != 2 && dim != 3) || !(d->settings.rmax > 0 && d->settings.rmax <= 1)) return -1;
     const int64_t nx = grid_n(d->settings.rmax);
     const int64_t cells = nx * nx * (dim == 3 ? nx : 1);
-    const int64_t per_particle = dim == 2 ? 2 * (16 + 8) + 4 * 4 : 2 * (16 + 16) + 4 * 4;
+    // two copies of position and velocity; cell, sort permutation, slot cell
+    const int64_t per_particle = dim == 2 ? 2 * (16 + 8) + 3 * 4 : 2 * (16 + 16) + 3 * 4;
     return d->n * per_particle + cells * 8 + (nx + 1) * 4 + (int64_t)d->ntypes * d->ntypes * 4;
 }
 
@@ -531,7 +531,6 @@ int plg_batch_create(int32_t dim, int64_t particle_capacity, int32_t world_capac
     dm(&b->avel, vel_sz * pc);
     dm(&b->bvel, vel_sz * pc);
     dm((void**)&b->cell, sizeof(uint32_t) * pc);
-    dm((void**)&b->rank, sizeof(uint32_t) * pc);
     dm((void**)&b->perm, sizeof(uint32_t) * pc);
     dm((void**)&b->slot_cell, sizeof(uint32_t) * pc);
     dm((void**)&b->counts, sizeof(uint32_t) * cc);
@@ -702,17 +701,17 @@ int plg_batch_autotune(plg_batch* b, int32_t steps, int32_t* chosen, double* ms_
         return PLG_OK;
     }
     const size_t vel_sz = b->dim == 2 ? sizeof(float2) : sizeof(float4);
-    const size_t bytes[5] = {sizeof(float4) * n, vel_sz * n, 4 * n, 4 * n, 4 * nc};
-    void* live[5] = {b->apt, b->avel, b->cell, b->rank, b->counts};
-    void* save[5] = {};
+    const size_t bytes[4] = {sizeof(float4) * n, vel_sz * n, 4 * n, 4 * nc};
+    void* live[4] = {b->apt, b->avel, b->cell, b->counts};
+    void* save[4] = {};
     int rc = PLG_OK;
-    for (int k = 0; k < 5 && !rc; ++k)
+    for (int k = 0; k < 4 && !rc; ++k)
         if (cudaMalloc(&save[k], bytes[k]) != cudaSuccess) {
             cudaGetLastError();
             rc = berr(b, PLG_E_NO_MEMORY, "cudaMalloc (autotune state copy)");
         }
     auto copy_all = [&](bool restore) -> cudaError_t {
-        for (int k = 0; k < 5; ++k) {
+        for (int k = 0; k < 4; ++k) {
             // A and B swap only in plg_batch_update, so `live` stays valid.
             cudaError_t e = cudaMemcpyAsync(restore ? live[k] : save[k], restore ? save[k] : live[k], bytes[k],
                                             cudaMemcpyDeviceToDevice, st);

@@ -2,12 +2,12 @@
 // (backend/Physics.java:309-354), plus the host-layout conversion kernels.
 //
 // Per step (after the force kernel of the previous step, or the upload, has
-// written every particle's cell and an in-cell rank and bumped the per-cell
-// counts):
+// written every particle's cell and bumped the per-cell counts):
 //   scan      counts -> exclusive offsets (Physics.java:334-340), single
-//             pass with decoupled look-back; counts reset
-//   scatter   perm[cstart[cell]+rank] = i (unstable: atomics order warps),
-//             and the cell of that slot
+//             pass with decoupled look-back
+//   scatter   perm[cstart[cell] + r] = i with an in-cell rank r taken from
+//             the counts (unstable: atomics order warps; the counts drain
+//             back to zero), and the cell of that slot
 //   gather    rank_stable(i) = #{members of i's cell with a smaller index};
 //             B[cstart[cell] + rank_stable] = A[i]
 // The gather makes the sort stable, so the cell-sorted order equals the one
@@ -62,9 +62,8 @@ __global__ void __launch_bounds__(kThreads) k_upload(int n, const double* __rest
                                                      const double* __restrict__ vel,
                                                      const int32_t* __restrict__ type, int ntypes,
                                                      StateBuf<D> a, uint32_t* __restrict__ cell,
-                                                     uint32_t* __restrict__ rank, uint32_t* counts, Grid g,
-                                                     uint32_t* status, bool vec, uint32_t cell_base,
-                                                     int id_base) {
+                                                     uint32_t* counts, Grid g, uint32_t* status, bool vec,
+                                                     uint32_t cell_base, int id_base) {
     __shared__ __align__(16) double sp[3 * kThreads];
     __shared__ __align__(16) double sv[3 * kThreads];
     const int i0 = blockIdx.x * kThreads;
@@ -117,7 +116,7 @@ __global__ void __launch_bounds__(kThreads) k_upload(int n, const double* __rest
     }
     const unsigned mask = __ballot_sync(kFull, valid);
     if (valid) {
-        rank[i] = bin_count(counts, c, mask);
+        bin_add(counts, c, mask);
         cell[i] = c;
     }
 }
@@ -139,8 +138,7 @@ __global__ void __launch_bounds__(kThreads) k_batch_move(int n, const int* __res
 template <int D>
 __global__ void __launch_bounds__(kThreads) k_batch_rebin(int n, StateBuf<D> a, const ForceParams* __restrict__ worlds,
                                                           const int* __restrict__ wp_off, int nw,
-                                                          uint32_t* __restrict__ cell, uint32_t* __restrict__ rank,
-                                                          uint32_t* counts) {
+                                                          uint32_t* __restrict__ cell, uint32_t* counts) {
     const int i = blockIdx.x * kThreads + threadIdx.x;
     const bool valid = i < n;
     uint32_t c = 0;
@@ -151,7 +149,7 @@ __global__ void __launch_bounds__(kThreads) k_batch_rebin(int n, StateBuf<D> a, 
     }
     const unsigned mask = __ballot_sync(kFull, valid);
     if (valid) {
-        rank[i] = bin_count(counts, c, mask);
+        bin_add(counts, c, mask);
         cell[i] = c;
     }
 }
@@ -164,7 +162,7 @@ __global__ void k_batch_tick(int* steps_left, int nworlds) {
 // Re-binning of the current state (after an rmax change).
 template <int D>
 __global__ void __launch_bounds__(kThreads) k_rebin(int n, StateBuf<D> a, uint32_t* __restrict__ cell,
-                                                    uint32_t* __restrict__ rank, uint32_t* counts, Grid g) {
+                                                    uint32_t* counts, Grid g) {
     const int i = blockIdx.x * kThreads + threadIdx.x;
     const bool valid = i < n;
     uint32_t c = 0;
@@ -174,7 +172,7 @@ __global__ void __launch_bounds__(kThreads) k_rebin(int n, StateBuf<D> a, uint32
     }
     const unsigned mask = __ballot_sync(kFull, valid);
     if (valid) {
-        rank[i] = bin_count(counts, c, mask);
+        bin_add(counts, c, mask);
         cell[i] = c;
     }
 }
@@ -261,10 +259,10 @@ __device__ __forceinline__ unsigned long long load_volatile(const unsigned long 
 // tile id, publishes its tile sum, and adds the sums of earlier tiles until it
 // meets a published inclusive prefix.  Tile ids follow block start order, so
 // a block only waits on blocks that are already running; every wait is
-// bounded and raises kDevSpinLimit instead of hanging.  Counts are reset to
-// zero for the next counting pass.  state[0] is the tile counter and
+// bounded and raises kDevSpinLimit instead of hanging.  The counts stay
+// (the scatter drains them).  state[0] is the tile counter and
 // state[1 + t] the status word of tile t; both start at zero each step.
-__global__ void __launch_bounds__(kScanThreads) k_scan(uint32_t* __restrict__ counts, int ncells,
+__global__ void __launch_bounds__(kScanThreads) k_scan(const uint32_t* __restrict__ counts, int ncells,
                                                        uint32_t* __restrict__ cstart, unsigned long long* state,
                                                        uint32_t* status, uint32_t* zero_word) {
     __shared__ uint32_t s_tile, s_prefix, total;
@@ -334,7 +332,6 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(uint32_t* __restrict__ co
         o.z = o.y + v[1];
         o.w = o.z + v[2];
         *reinterpret_cast<uint4*>(cstart + base) = o;
-        *reinterpret_cast<uint4*>(counts + base) = make_uint4(0u, 0u, 0u, 0u);
         if (base + kScanItems == ncells) cstart[ncells] = o.w + v[3];
     } else {
 #pragma unroll
@@ -342,7 +339,6 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(uint32_t* __restrict__ co
             const int c = base + k;
             if (c < ncells) {
                 cstart[c] = run;
-                counts[c] = 0;
                 if (c == ncells - 1) cstart[ncells] = run + v[k];
             }
             run += v[k];
@@ -350,14 +346,17 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(uint32_t* __restrict__ co
     }
 }
 
-__global__ void __launch_bounds__(kThreads) k_scatter(int n, const uint32_t* __restrict__ cell,
-                                                      const uint32_t* __restrict__ rank,
+// Each particle takes a slot of its cell (the ranks drain counts back to
+// zero for the next counting pass).
+__global__ void __launch_bounds__(kThreads) k_scatter(int n, const uint32_t* __restrict__ cell, uint32_t* counts,
                                                       const uint32_t* __restrict__ cstart,
                                                       uint32_t* __restrict__ perm, uint32_t* __restrict__ slot_cell) {
     const int i = blockIdx.x * kThreads + threadIdx.x;
-    if (i >= n) return;
-    const uint32_t c = cell[i];
-    const uint32_t slot = cstart[c] + rank[i];
+    const bool valid = i < n;
+    const uint32_t c = valid ? cell[i] : 0u;
+    const unsigned mask = __ballot_sync(kFull, valid);
+    if (!valid) return;
+    const uint32_t slot = __ldg(cstart + c) + bin_take(counts, c, mask);
     perm[slot] = (uint32_t)i;
     if (slot_cell) slot_cell[slot] = c;
 }
@@ -392,12 +391,12 @@ inline bool aligned16(const void* p) { return ((uintptr_t)p & 15u) == 0; }
 
 template <int D>
 void launch_upload(cudaStream_t st, int n, const double* pos, const double* vel, const int32_t* type, int ntypes,
-                   StateBuf<D> a, uint32_t* cell, uint32_t* rank, uint32_t* counts, Grid g, uint32_t* status,
-                   uint32_t cell_base, int id_base) {
+                   StateBuf<D> a, uint32_t* cell, uint32_t* counts, Grid g, uint32_t* status, uint32_t cell_base,
+                   int id_base) {
     if (n <= 0) return;
     const bool vec = aligned16(pos) && aligned16(vel);
-    k_upload<D><<<blocks_for(n, kThreads), kThreads, 0, st>>>(n, pos, vel, type, ntypes, a, cell, rank, counts, g,
-                                                              status, vec, cell_base, id_base);
+    k_upload<D><<<blocks_for(n, kThreads), kThreads, 0, st>>>(n, pos, vel, type, ntypes, a, cell, counts, g, status,
+                                                              vec, cell_base, id_base);
 }
 
 template <int D>
@@ -409,9 +408,9 @@ void launch_batch_move(cudaStream_t st, int n, const int* new_off, const int* ol
 
 template <int D>
 void launch_batch_rebin(cudaStream_t st, int n, StateBuf<D> a, const ForceParams* worlds, const int* wp_off, int nw,
-                        uint32_t* cell, uint32_t* rank, uint32_t* counts) {
+                        uint32_t* cell, uint32_t* counts) {
     if (n <= 0 || nw <= 0) return;
-    k_batch_rebin<D><<<blocks_for(n, kThreads), kThreads, 0, st>>>(n, a, worlds, wp_off, nw, cell, rank, counts);
+    k_batch_rebin<D><<<blocks_for(n, kThreads), kThreads, 0, st>>>(n, a, worlds, wp_off, nw, cell, counts);
 }
 
 void launch_batch_tick(cudaStream_t st, int* steps_left, int nworlds) {
@@ -422,14 +421,14 @@ void launch_batch_tick(cudaStream_t st, int* steps_left, int nworlds) {
 template void launch_batch_move<2>(cudaStream_t, int, const int*, const int*, int, StateBuf<2>, StateBuf<2>);
 template void launch_batch_move<3>(cudaStream_t, int, const int*, const int*, int, StateBuf<3>, StateBuf<3>);
 template void launch_batch_rebin<2>(cudaStream_t, int, StateBuf<2>, const ForceParams*, const int*, int, uint32_t*,
-                                    uint32_t*, uint32_t*);
+                                    uint32_t*);
 template void launch_batch_rebin<3>(cudaStream_t, int, StateBuf<3>, const ForceParams*, const int*, int, uint32_t*,
-                                    uint32_t*, uint32_t*);
+                                    uint32_t*);
 
 template <int D>
-void launch_rebin(cudaStream_t st, int n, StateBuf<D> a, uint32_t* cell, uint32_t* rank, uint32_t* counts, Grid g) {
+void launch_rebin(cudaStream_t st, int n, StateBuf<D> a, uint32_t* cell, uint32_t* counts, Grid g) {
     if (n <= 0) return;
-    k_rebin<D><<<blocks_for(n, kThreads), kThreads, 0, st>>>(n, a, cell, rank, counts, g);
+    k_rebin<D><<<blocks_for(n, kThreads), kThreads, 0, st>>>(n, a, cell, counts, g);
 }
 
 template <int D>
@@ -441,15 +440,15 @@ void launch_download(cudaStream_t st, int n, StateBuf<D> a, double* pos, double*
 
 int scan_blocks(int ncells) { return blocks_for(ncells, kScanTile); }
 
-void launch_scan(cudaStream_t st, uint32_t* counts, int ncells, uint32_t* cstart, unsigned long long* state,
+void launch_scan(cudaStream_t st, const uint32_t* counts, int ncells, uint32_t* cstart, unsigned long long* state,
                  uint32_t* status, uint32_t* zero_word) {
     k_scan<<<scan_blocks(ncells), kScanThreads, 0, st>>>(counts, ncells, cstart, state, status, zero_word);
 }
 
-void launch_scatter(cudaStream_t st, int n, const uint32_t* cell, const uint32_t* rank, const uint32_t* cstart,
+void launch_scatter(cudaStream_t st, int n, const uint32_t* cell, uint32_t* counts, const uint32_t* cstart,
                     uint32_t* perm, uint32_t* slot_cell) {
     if (n <= 0) return;
-    k_scatter<<<blocks_for(n, kThreads), kThreads, 0, st>>>(n, cell, rank, cstart, perm, slot_cell);
+    k_scatter<<<blocks_for(n, kThreads), kThreads, 0, st>>>(n, cell, counts, cstart, perm, slot_cell);
 }
 
 template <int D>
@@ -460,11 +459,11 @@ void launch_gather(cudaStream_t st, int n, const uint32_t* perm, const uint32_t*
 }
 
 template void launch_upload<2>(cudaStream_t, int, const double*, const double*, const int32_t*, int, StateBuf<2>,
-                               uint32_t*, uint32_t*, uint32_t*, Grid, uint32_t*, uint32_t, int);
+                               uint32_t*, uint32_t*, Grid, uint32_t*, uint32_t, int);
 template void launch_upload<3>(cudaStream_t, int, const double*, const double*, const int32_t*, int, StateBuf<3>,
-                               uint32_t*, uint32_t*, uint32_t*, Grid, uint32_t*, uint32_t, int);
-template void launch_rebin<2>(cudaStream_t, int, StateBuf<2>, uint32_t*, uint32_t*, uint32_t*, Grid);
-template void launch_rebin<3>(cudaStream_t, int, StateBuf<3>, uint32_t*, uint32_t*, uint32_t*, Grid);
+                               uint32_t*, uint32_t*, Grid, uint32_t*, uint32_t, int);
+template void launch_rebin<2>(cudaStream_t, int, StateBuf<2>, uint32_t*, uint32_t*, Grid);
+template void launch_rebin<3>(cudaStream_t, int, StateBuf<3>, uint32_t*, uint32_t*, Grid);
 template void launch_download<2>(cudaStream_t, int, StateBuf<2>, double*, double*, int32_t*, int32_t*);
 template void launch_download<3>(cudaStream_t, int, StateBuf<3>, double*, double*, int32_t*, int32_t*);
 template void launch_gather<2>(cudaStream_t, int, const uint32_t*, const uint32_t*, const uint32_t*, StateBuf<2>,

@@ -62,10 +62,10 @@ struct ForceArgs {
     const float4* __restrict__ bpt;
     const typename Layout<D>::Vel* __restrict__ bvel;
     const uint32_t* __restrict__ cstart;
+    const uint32_t* __restrict__ slot_cell;  // cell of each slot of B (the sort's), with cell_base
     float4* __restrict__ apt;
     typename Layout<D>::Vel* __restrict__ avel;
     uint32_t* __restrict__ cell;
-    uint32_t* __restrict__ rank;
     uint32_t* counts;
     uint32_t* defer_count;  // targets the tiled kernel deferred this step (statistics)
     DebugOut dbg;
@@ -366,13 +366,12 @@ __device__ __forceinline__ float ensure_position(float x, int wrap) {
     return fminf(fmaxf(x, 0.f), 1.f);
 }
 
-// Epilogue of one target (sorted slot s): v = v ff + acc (rmax force dt),
+// Epilogue of one target (sorted slot s, velocity v): v = v ff + acc (rmax force dt),
 // x = v dt + x, ensurePosition; the next state goes to A[s].  Returns the
 // new cell.
 template <int D, bool DBG>
 __device__ __forceinline__ uint32_t integrate(const ForceArgs<D>& A, const ForceParams& P, int s, const float4& me,
-                                              const Acc& acc) {
-    typename Layout<D>::Vel v = A.bvel[s];
+                                              const typename Layout<D>::Vel& v, const Acc& acc) {
     const float vx = fmaf(acc.x, P.scale, v.x * P.ff);
     const float vy = fmaf(acc.y, P.scale, v.y * P.ff);
     const float nxp = ensure_position(__fadd_rn(__fmul_rn(vx, P.dt), me.x), P.wrap);
@@ -427,11 +426,11 @@ __global__ void __launch_bounds__(kThreads) k_force_general(const __grid_constan
         const float4 me = A.bpt[s];
         Acc acc = {0.f, 0.f, 0.f, 0, 0ull, 0ull, 0ull};
         general_scan<D, DBG>(A, M + Layout<D>::type(me) * P.ntypes, s, me.x, me.y, D == 3 ? me.z : 0.f, acc);
-        newcell = integrate<D, DBG>(A, A.p, s, me, acc);
+        newcell = integrate<D, DBG>(A, A.p, s, me, A.bvel[s], acc);
     }
     const unsigned mask = __ballot_sync(kFull, valid);
     if (valid) {
-        A.rank[s] = bin_count(A.counts, newcell, mask);
+        bin_add(A.counts, newcell, mask);
         A.cell[s] = newcell;
     }
 }
@@ -445,7 +444,8 @@ struct TileRows {
 
 // Tile variants (the autotuner's choice, PLG_TILE_*):
 //   kTargets    targets per block, one thread each
-//   kMinBlocks  resident blocks per SM the shared memory allows (caps registers)
+//   kMinBlocks  resident blocks per SM asked for (caps the registers: more
+//               blocks with spilled registers measured slower)
 //   kCap        staged candidates per segment
 //   kCells      stencil cells per segment (R x columns)
 // Variant 0 suits dense worlds; variant 1 (smaller tiles, less shared memory,
@@ -454,7 +454,7 @@ template <int D, int V>
 struct TileCfg;
 template <>
 struct TileCfg<2, 0> {
-    static constexpr int kTargets = 256, kMinBlocks = 6, kCap = 1536, kCells = 512;
+    static constexpr int kTargets = 256, kMinBlocks = 4, kCap = 1536, kCells = 512;
 };
 template <>
 struct TileCfg<2, 1> {
@@ -462,7 +462,7 @@ struct TileCfg<2, 1> {
 };
 template <>
 struct TileCfg<3, 0> {
-    static constexpr int kTargets = 128, kMinBlocks = 6, kCap = 1536, kCells = 512;
+    static constexpr int kTargets = 128, kMinBlocks = 5, kCap = 2048, kCells = 512;
 };
 template <>
 struct TileCfg<3, 1> {
@@ -474,18 +474,26 @@ struct TileCfg<3, 1> {
 // the periodic image above the box of a cell near coordinate 0.
 constexpr int kShiftX = 1 << 16, kShiftY = 1 << 17, kShiftZ = 1 << 18;
 
-// Lives in dynamic shared memory (variant 0: about 31 KB in 2D, 31 KB in 3D).
+// Lives in dynamic shared memory (variant 0: about 35 KB in 2D, 41 KB in 3D).
+// Staged columns: the sorted union of the windows cx-1..cx+1 of the staged
+// targets, as "virtual" columns -1..nx (-1 and nx being the periodic images
+// of columns nx-1 and 0), each with the grid row of its segment.
 template <int D, int V>
 struct TileSmem {
+    static constexpr int kCols = TileCfg<D, V>::kCells / TileRows<D>::R;
     float4 cand[TileCfg<D, V>::kCap];      // staged candidates, column-major by stencil cell
     int coff[TileCfg<D, V>::kCells + 1];   // smem start of stencil cell e = column * R + row
     int cglob[TileCfg<D, V>::kCells];      // sorted-order start of stencil cell e
+    int colv[kCols];                       // virtual column of staged column ci
+    int colrow[kCols];                     // grid row (y, or y + z nx) of staged column ci
     int rowid[TileCfg<D, V>::kTargets];
     int colid[TileCfg<D, V>::kTargets];
-    int seg[TileCfg<D, V>::kTargets + 1];
+    int seg[TileCfg<D, V>::kTargets + 1];  // first target of each segment
+    int segc[TileCfg<D, V>::kTargets + 1]; // first window column of each segment
     int wsum[TileCfg<D, V>::kTargets / 32];
+    int wcol[TileCfg<D, V>::kTargets / 32];
     int nseg;
-    int staged;                         // 1: the segment's stencil is in smem
+    int staged;                         // 1: the staged columns' candidates are in smem
     float mat[kSmemMatrixMax * kSmemMatrixMax];
 };
 
@@ -531,77 +539,118 @@ __device__ __forceinline__ int block_scan_inplace(int* v, int n, int* wsum) {
     return total;
 }
 
-// Stages the stencil of the segment (grid row `srow`, columns cxa..cxb),
-// column-major: for each stencil column (cxa-1 .. cxb+1) the cells of its R
-// stencil rows in turn, so that the neighbourhood of a target in column cx is
-// the single contiguous range of columns cx-1 .. cx+1.  Images below the box
-// are shifted down by 1 here (exact: their coordinates are >= 0.5); images
-// above it are flagged for a target shift instead.
+// A staged candidate: coordinates of an image below the box moved down by
+// one, target-shift flags (images above the box) in the type word.
+template <int D>
+__device__ __forceinline__ float4 shift_candidate(float4 q, float sx, float sy, float sz, int flags) {
+    q.x -= sx;
+    q.y -= sy;
+    if (D == 3) q.z -= sz;
+    if constexpr (D == 2)
+        q.z = __int_as_float(__float_as_int(q.z) | flags);
+    else
+        q.w = __int_as_float(__float_as_int(q.w) | flags);
+    return q;
+}
+
+// Stages the cells of staged columns 0..ncols-1 (sm.colv, sm.colrow),
+// column-major: for each column the cells of its R stencil rows in turn, so
+// that the neighbourhood of a target whose window starts at column k is the
+// single contiguous range of columns k .. k+2.  Images below the box are
+// shifted down by 1 here (exact: their coordinates are >= 0.5); images above
+// it are flagged for a target shift instead.  Thread t owns cells
+// t*per .. t*per+per-1: it reads their extents, the block scans the
+// per-thread sums, and the owner copies its cells.  Returns whether the
+// candidates fit (every thread gets the same answer); ncols * R <= kCells
+// is the caller's.
 template <int D, int V>
-__device__ __forceinline__ void stage_segment(const ForceArgs<D>& A, const ForceParams& P,
-                                              const uint32_t* __restrict__ cs, TileSmem<D, V>& sm, int srow, int cxa,
-                                              int cxb) {
+__device__ __forceinline__ bool stage_columns(const ForceArgs<D>& A, const ForceParams& P,
+                                              const uint32_t* __restrict__ cs, TileSmem<D, V>& sm, int ncols) {
     constexpr int R = TileRows<D>::R;
+    constexpr int kT = TileCfg<D, V>::kTargets;
+    constexpr int kPer = (TileCfg<D, V>::kCells + kT - 1) / kT;
     const int nx = P.g.nx;
-    const int tid = threadIdx.x;
-    const int cy = D == 3 ? srow % nx : srow, cz = D == 3 ? srow / nx : 0;
-    const int ncols = cxb - cxa + 1;
-    const int ncell = R * (ncols + 2);
-    if (ncell > TileCfg<D, V>::kCells) {
-        if (tid == 0) sm.staged = 0;
-        __syncthreads();
-        return;
-    }
-    for (int e = tid; e < ncell; e += TileCfg<D, V>::kTargets) {
-        const int ci = e / R, r = e - ci * R;
-        const int col = wrap_index(cxa - 1 + ci, nx);
-        const int ry = wrap_index(cy + r % 3 - 1, nx);
-        const int rz = D == 3 ? wrap_index(cz + r / 3 - 1, nx) : 0;
-        const int c = (rz * nx + ry) * nx + col;
-        const int g0 = (int)__ldg(cs + c);
-        sm.cglob[e] = g0;
-        sm.coff[e] = (int)__ldg(cs + c + 1) - g0;
-    }
-    __syncthreads();
-    const int total = block_scan_inplace<D, V>(sm.coff, ncell, sm.wsum);
-    if (tid == 0) {
-        sm.coff[ncell] = total;
-        sm.staged = total <= TileCfg<D, V>::kCap;
-    }
-    __syncthreads();
-    if (!sm.staged) return;
-    for (int k = tid; k < total; k += TileCfg<D, V>::kTargets) {
-        int lo = 0, hi = ncell;  // last e with coff[e] <= k
-        while (hi - lo > 1) {
-            const int m = (lo + hi) >> 1;
-            if (sm.coff[m] <= k)
-                lo = m;
-            else
-                hi = m;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int ncell = R * ncols;
+    const int per = (ncell + kT - 1) / kT;
+    int g0[kPer], len[kPer];
+    int sum = 0;
+#pragma unroll
+    for (int i = 0; i < kPer; ++i) {
+        const int e = tid * per + i;
+        g0[i] = 0;
+        len[i] = 0;
+        if (i < per && e < ncell) {
+            const int ci = e / R, r = e - ci * R;
+            const int col = wrap_index(sm.colv[ci], nx);
+            const int row = sm.colrow[ci];
+            const int cy = D == 3 ? row % nx : row, cz = D == 3 ? row / nx : 0;
+            const int ry = wrap_index(cy + r % 3 - 1, nx);
+            const int rz = D == 3 ? wrap_index(cz + r / 3 - 1, nx) : 0;
+            const int c = (rz * nx + ry) * nx + col;
+            g0[i] = (int)__ldg(cs + c);
+            len[i] = (int)__ldg(cs + c + 1) - g0[i];
         }
-        const int e = lo, ci = e / R, r = e - ci * R;
-        float4 q = __ldg(A.bpt + sm.cglob[e] + (k - sm.coff[e]));
-        if (P.wrap) {
-            const int oy = r % 3 - 1, oz = D == 3 ? r / 3 - 1 : 0;
+        sum += len[i];
+    }
+    int inc = sum;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const int t = __shfl_up_sync(kFull, inc, d);
+        if (lane >= d) inc += t;
+    }
+    if (lane == 31) sm.wsum[warp] = inc;
+    __syncthreads();
+    int before = 0, total = 0;
+#pragma unroll
+    for (int w = 0; w < kT / 32; ++w) {
+        const int x = sm.wsum[w];
+        before += w < warp ? x : 0;
+        total += x;
+    }
+    if (total > TileCfg<D, V>::kCap) return false;  // block-uniform
+    int run = before + inc - sum;
+#pragma unroll
+    for (int i = 0; i < kPer; ++i) {
+        const int e = tid * per + i;
+        if (i < per && e < ncell) {
+            sm.cglob[e] = g0[i];
+            sm.coff[e] = run;
+            if (e == ncell - 1) sm.coff[ncell] = run + len[i];
+            // The cell's image shifts.
+            const int ci = e / R, r = e - ci * R;
+            float sx = 0.f, sy = 0.f, sz = 0.f;
             int flags = 0;
-            if (ci == 0 && cxa == 0) q.x -= 1.f;
-            if (ci == ncols + 1 && cxb == nx - 1) flags |= kShiftX;
-            if (cy + oy < 0) q.y -= 1.f;
-            if (cy + oy >= nx) flags |= kShiftY;
-            if (D == 3) {
-                if (cz + oz < 0) q.z -= 1.f;
-                if (cz + oz >= nx) flags |= kShiftZ;
+            if (P.wrap) {
+                const int v = sm.colv[ci], row = sm.colrow[ci];
+                const int cy = D == 3 ? row % nx : row, cz = D == 3 ? row / nx : 0;
+                const int oy = r % 3 - 1, oz = D == 3 ? r / 3 - 1 : 0;
+                if (v < 0) sx = 1.f;
+                if (v >= nx) flags |= kShiftX;
+                if (cy + oy < 0) sy = 1.f;
+                if (cy + oy >= nx) flags |= kShiftY;
+                if (D == 3) {
+                    if (cz + oz < 0) sz = 1.f;
+                    if (cz + oz >= nx) flags |= kShiftZ;
+                }
             }
-            if (flags) {
-                if constexpr (D == 2)
-                    q.z = __int_as_float(__float_as_int(q.z) | flags);
-                else
-                    q.w = __int_as_float(__float_as_int(q.w) | flags);
+            const float4* __restrict__ src = A.bpt + g0[i];
+            float4* dst = sm.cand + run;
+            const int m = len[i];
+            int k = 0;
+            for (; k + 4 <= m; k += 4) {
+                float4 q[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) q[u] = __ldg(src + k + u);
+#pragma unroll
+                for (int u = 0; u < 4; ++u) dst[k + u] = shift_candidate<D>(q[u], sx, sy, sz, flags);
             }
+            for (; k < m; ++k) dst[k] = shift_candidate<D>(__ldg(src + k), sx, sy, sz, flags);
         }
-        sm.cand[k] = q;
+        run += len[i];
     }
     __syncthreads();
+    return true;
 }
 
 // Global sorted slot of staged candidate j (rare path and debug only).
@@ -799,8 +848,8 @@ __device__ __noinline__ void fixup_target(const ForceArgs<D>& A, const ForcePara
         }
     }
     if (lane == 0) {
-        const uint32_t newcell = integrate<D, DBG>(A, P, s, me, acc);
-        A.rank[s] = atomicAdd(A.counts + newcell, 1u);
+        const uint32_t newcell = integrate<D, DBG>(A, P, s, me, A.bvel[s], acc);
+        atomicAdd(A.counts + newcell, 1u);
         A.cell[s] = newcell;
     }
 }
@@ -848,7 +897,7 @@ __global__ void __launch_bounds__(TileCfg<D, V>::kTargets, TileCfg<D, V>::kMinBl
         uint32_t c = 0;
         if (valid) c = A.cell[s];
         const unsigned m = __ballot_sync(kFull, valid);
-        if (valid) A.rank[s] = bin_count(A.counts, c, m);
+        if (valid) bin_add(A.counts, c, m);
         return;
     }
     if (SMEM_M) {
@@ -857,99 +906,153 @@ __global__ void __launch_bounds__(TileCfg<D, V>::kTargets, TileCfg<D, V>::kMinBl
     }
     const float* M = SMEM_M ? sm.mat : P.matrix;
     float4 me = make_float4(0.f, 0.f, 0.f, 0.f);
+    typename Layout<D>::Vel vme{};
     int cx = 0, row = INT_MAX;
     if (valid) {
+        // The target's cell is the one the sort binned it by (computed from
+        // these same coordinates by the previous epilogue or the upload).
+        const uint32_t c = __ldg(A.slot_cell + s) - P.cell_base;
         me = A.bpt[s];
-        cx = axis_cell(me.x, P.g);
-        const int cy = axis_cell(me.y, P.g);
-        const int cz = D == 3 ? axis_cell(me.z, P.g) : 0;
-        row = cy + cz * P.g.nx;
+        vme = A.bvel[s];  // needed only by the epilogue: loaded early, off its critical path
+        const uint32_t nxu = (uint32_t)P.g.nx;
+        row = (int)(c / nxu);
+        cx = (int)(c - (uint32_t)row * nxu);
     }
     sm.rowid[tid] = row;
     sm.colid[tid] = cx;
     __syncthreads();
-    // Segments: maximal runs of targets in one grid row (rows are nondecreasing).
+    // Segments: maximal runs of targets in one grid row (rows are
+    // nondecreasing, and so are the columns within a segment).  Window
+    // columns: each first target of a column adds the columns of its window
+    // cx-1..cx+1 that the previous column's window has not added (3 at a
+    // segment start); a block-wide scan numbers them, so the target's window
+    // starts at staged column kwin = incl - 3.
+    const int lane = tid & 31, warp = tid >> 5;
+    const int pcol = tid > 0 ? sm.colid[tid - 1] : 0;
     const bool start = valid && (tid == 0 || sm.rowid[tid - 1] != row);
+    const bool lead = valid && (start || pcol != cx);
+    const int newc = !lead ? 0 : (start ? 3 : min(3, cx - pcol));
     const unsigned bal = __ballot_sync(kFull, start);
-    if ((tid & 31) == 0) sm.wsum[tid >> 5] = __popc(bal);
-    __syncthreads();
-    int before = 0;
-    for (int w = 0; w < (tid >> 5); ++w) before += sm.wsum[w];
-    if (start) sm.seg[before + __popc(bal & ((1u << (tid & 31)) - 1u))] = tid;
-    if (tid == 0) {
-        int t = 0;
-        for (int w = 0; w < kT / 32; ++w) t += sm.wsum[w];
-        sm.nseg = t;
-        sm.seg[t] = nvalid;
+    int incl = newc;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const int t = __shfl_up_sync(kFull, incl, d);
+        if (lane >= d) incl += t;
+    }
+    if (lane == 31) {
+        sm.wsum[warp] = __popc(bal);
+        sm.wcol[warp] = incl;
     }
     __syncthreads();
-    const int nseg = sm.nseg;
-
+    int sbefore = 0, stotal = 0, cbefore = 0, ncol = 0;
+#pragma unroll
+    for (int w = 0; w < kT / 32; ++w) {
+        const int x = sm.wsum[w], y = sm.wcol[w];
+        sbefore += w < warp ? x : 0;
+        cbefore += w < warp ? y : 0;
+        stotal += x;
+        ncol += y;
+    }
+    incl += cbefore;
+    const int kwin = incl - 3;
+    // Staged columns [cb, ce) of the block numbering, as 0 .. ce-cb-1.
+    auto fill_columns = [&](int cb, int ce) {
+        for (int i = 0; i < newc; ++i) {
+            const int ci = incl - newc + i;
+            if (ci >= cb && ci < ce) {
+                sm.colv[ci - cb] = cx + 2 - newc + i;
+                sm.colrow[ci - cb] = row;
+            }
+        }
+    };
+    constexpr int kCols = TileSmem<D, V>::kCols;
+    // One staging for the whole block when every window fits; otherwise per
+    // segment, in chunks (below).
+    bool whole = ncol <= kCols;  // block-uniform
+    if (whole) fill_columns(0, ncol);
+    if (start) {
+        const int g = sbefore + __popc(bal & ((1u << lane) - 1u));
+        sm.seg[g] = tid;
+        sm.segc[g] = kwin;
+    }
+    if (tid == 0) sm.segc[stotal] = ncol;
+    const int nx = P.g.nx;
+    const int cy = D == 3 ? (valid ? row % nx : 0) : row, cz = D == 3 ? (valid ? row / nx : 0) : 0;
     const float px = me.x, py = me.y, pz = D == 3 ? me.z : 0.f;
     const float* Mrow = M + (valid ? Layout<D>::type(me) : 0) * P.ntypes;
     Acc acc = {0.f, 0.f, 0.f, 0, 0ull, 0ull, 0ull};
     bool defer = false, direct = false;
-    for (int g = 0; g < nseg; ++g) {
-        const int ta = sm.seg[g], tb = sm.seg[g + 1];
-        const int srow = sm.rowid[ta];
-        const int cxa = sm.colid[ta], cxb = sm.colid[tb - 1];
-        stage_segment<D, V>(A, P, A.cstart + P.cell_base, sm, srow, cxa, cxb);
-        if (tid >= ta && tid < tb) {
-            if (sm.staged) {
-                const int nx = P.g.nx;
-                const int ncell = R * (cxb - cxa + 3);
-                const int k = cx - cxa + 1;  // stencil column of the target
-                const int j0 = sm.coff[(k - 1) * R], j1 = sm.coff[(k + 2) * R];
-                const int own = k * R + R / 2;
-                const int self_j = sm.coff[own] + (s - sm.cglob[own]);
-                const int cy = D == 3 ? srow % nx : srow, cz = D == 3 ? srow / nx : 0;
-                const bool shift = P.wrap && (cxb == nx - 1 || cy == nx - 1 || (D == 3 && cz == nx - 1));
-                // The target itself splits its run: [j0, self_j) and (self_j, j1).
-                if (shift) {
-                    defer = tile_range<D, DBG, true, V>(A, P, sm, Mrow, ncell, j0, self_j, px, py, pz, acc);
-                    defer |= tile_range<D, DBG, true, V>(A, P, sm, Mrow, ncell, self_j + 1, j1, px, py, pz, acc);
+    // The target's window: staged columns k .. k+2; the target itself splits
+    // its run into [j0, self_j) and (self_j, j1).  Only a target in the last
+    // column, row or layer of a periodic box meets candidates flagged for a
+    // target shift.
+    auto evaluate = [&](int k, int ncell) {
+        const int j0 = sm.coff[k * R], j1 = sm.coff[(k + 3) * R];
+        const int own = (k + 1) * R + R / 2;
+        const int self_j = sm.coff[own] + (s - sm.cglob[own]);
+        const bool shift = P.wrap && (cx == nx - 1 || cy == nx - 1 || (D == 3 && cz == nx - 1));
+        if (shift) {
+            defer = tile_range<D, DBG, true, V>(A, P, sm, Mrow, ncell, j0, self_j, px, py, pz, acc);
+            defer |= tile_range<D, DBG, true, V>(A, P, sm, Mrow, ncell, self_j + 1, j1, px, py, pz, acc);
+        } else {
+            defer = tile_range<D, DBG, false, V>(A, P, sm, Mrow, ncell, j0, self_j, px, py, pz, acc);
+            defer |= tile_range<D, DBG, false, V>(A, P, sm, Mrow, ncell, self_j + 1, j1, px, py, pz, acc);
+        }
+    };
+    __syncthreads();
+    const uint32_t* cs = A.cstart + P.cell_base;
+    if (whole) {
+        whole = stage_columns<D, V>(A, P, cs, sm, ncol);
+        if (whole && valid) evaluate(kwin, R * ncol);
+    }
+    if (!whole) {
+        // Per segment, in chunks of window columns [a, hi) serving the
+        // targets whose window starts in [a, hi - 3]; a chunk whose
+        // candidates do not fit is retried with half as many columns, and a
+        // single window that does not fit is read from global memory.
+        for (int g = 0; g < stotal; ++g) {
+            const int cb = sm.segc[g], ce = sm.segc[g + 1];
+            int a = cb, width = min(ce - cb, kCols);
+            while (a <= ce - 3) {
+                const int hi = min(a + width, ce);
+                fill_columns(a, hi);  // the previous staging no longer reads the columns
+                __syncthreads();
+                const bool staged = stage_columns<D, V>(A, P, cs, sm, hi - a);
+                const bool mine = valid && kwin >= a && kwin <= hi - 3;
+                if (staged) {
+                    if (mine) evaluate(kwin - a, R * (hi - a));
+                    a = hi - 2;
+                } else if (hi - a > 3) {
+                    width = max(3, (hi - a) / 2);
                 } else {
-                    defer = tile_range<D, DBG, false, V>(A, P, sm, Mrow, ncell, j0, self_j, px, py, pz, acc);
-                    defer |= tile_range<D, DBG, false, V>(A, P, sm, Mrow, ncell, self_j + 1, j1, px, py, pz, acc);
+                    if (mine) direct = true;  // computed after the loop, off the hot path
+                    a += 1;
                 }
-            } else {
-                direct = true;  // computed after the loop, off the hot path
             }
         }
-        if (g + 1 < nseg) __syncthreads();  // staging of the next segment reuses smem
     }
     if (direct) {
-        // The segment did not fit in shared memory: the same sum from
-        // global memory.
-        const int cy = axis_cell(py, P.g), cz = D == 3 ? axis_cell(pz, P.g) : 0;
-        defer = direct_stencil<D, DBG>(A, P, A.cstart + P.cell_base, Mrow, s, px, py, pz, cx, cy, cz, acc);
+        // The window did not fit in shared memory: the same sum from global
+        // memory.
+        defer = direct_stencil<D, DBG>(A, P, cs, Mrow, s, px, py, pz, cx, cy, cz, acc);
     }
     const bool done = valid && !defer;
     uint32_t newcell = 0;
-    if (done) newcell = integrate<D, DBG>(A, P, s, me, acc);
+    if (done) newcell = integrate<D, DBG>(A, P, s, me, vme, acc);
     const unsigned mask = __ballot_sync(kFull, done);
     if (done) {
-        A.rank[s] = bin_count(A.counts, newcell, mask);
+        bin_add(A.counts, newcell, mask);
         A.cell[s] = newcell;
     }
-    // Deferred targets of this block (FP64 band pairs), one warp each, from
-    // global memory.  Most blocks have none.
-    const int warp = tid >> 5, lane = tid & 31;
-    const unsigned dm = __ballot_sync(kFull, valid && defer);
-    __syncthreads();  // rowid and wsum are free again
-    if (lane == 0) sm.wsum[warp] = __popc(dm);
-    __syncthreads();
-    int nd = 0, dbefore = 0;
-    for (int w = 0; w < kT / 32; ++w) {
-        const int x = sm.wsum[w];
-        dbefore += w < warp ? x : 0;
-        nd += x;
+    // Deferred targets (FP64 band pairs): each warp recomputes its own, one
+    // at a time, from global memory.  Most warps have none.
+    unsigned dm = __ballot_sync(kFull, valid && defer);
+    if (dm && lane == 0) atomicAdd(A.defer_count, (uint32_t)__popc(dm));
+    while (dm) {
+        const int src = __ffs(dm) - 1;
+        dm &= dm - 1;
+        fixup_target<D, DBG>(A, P, cs, M, __shfl_sync(kFull, s, src), lane);
     }
-    if (nd == 0) return;  // block-uniform
-    if (valid && defer) sm.rowid[dbefore + __popc(dm & ((1u << lane) - 1u))] = s;
-    if (tid == 0) atomicAdd(A.defer_count, (uint32_t)nd);
-    __syncthreads();
-    for (int d = warp; d < nd; d += kT / 32) fixup_target<D, DBG>(A, P, A.cstart + P.cell_base, M, sm.rowid[d], lane);
 }
 
 template <int D, bool DBG, bool BATCH, int V>
@@ -989,17 +1092,17 @@ void launch_variant(cudaStream_t st, const ForceArgs<D>& A, bool general, int va
 }
 
 template <int D>
-ForceArgs<D> make_args(const ForceParams& p, StateBuf<D> b, const uint32_t* cstart, StateBuf<D> a, uint32_t* cell,
-                       uint32_t* rank, uint32_t* counts, uint32_t* defer, const DebugOut* dbg) {
+ForceArgs<D> make_args(const ForceParams& p, StateBuf<D> b, const uint32_t* cstart, const uint32_t* slot_cell,
+                       StateBuf<D> a, uint32_t* cell, uint32_t* counts, uint32_t* defer, const DebugOut* dbg) {
     ForceArgs<D> A;
     A.p = p;
     A.bpt = b.pt;
     A.bvel = b.vel;
     A.cstart = cstart;
+    A.slot_cell = slot_cell;
     A.apt = a.pt;
     A.avel = a.vel;
     A.cell = cell;
-    A.rank = rank;
     A.counts = counts;
     A.defer_count = defer;
     A.dbg = dbg ? *dbg : DebugOut{nullptr, nullptr, nullptr, nullptr, nullptr};
@@ -1016,10 +1119,10 @@ ForceArgs<D> make_args(const ForceParams& p, StateBuf<D> b, const uint32_t* csta
 
 template <int D>
 void launch_force(cudaStream_t st, const ForceParams& p, bool general, StateBuf<D> b, const uint32_t* cstart,
-                  StateBuf<D> a, uint32_t* cell, uint32_t* rank, uint32_t* counts, uint32_t* defer,
+                  const uint32_t* slot_cell, StateBuf<D> a, uint32_t* cell, uint32_t* counts, uint32_t* defer,
                   const DebugOut* dbg, int variant) {
     if (p.n <= 0) return;
-    const ForceArgs<D> A = make_args<D>(p, b, cstart, a, cell, rank, counts, defer, dbg);
+    const ForceArgs<D> A = make_args<D>(p, b, cstart, slot_cell, a, cell, counts, defer, dbg);
     if (dbg)
         launch_variant<D, true>(st, A, general, variant);
     else
@@ -1029,11 +1132,11 @@ void launch_force(cudaStream_t st, const ForceParams& p, bool general, StateBuf<
 template <int D>
 void launch_force_batch(cudaStream_t st, const ForceParams* worlds, const int* wp_off, const int* tile_off,
                         const int* steps_left, int tiles, int nworlds, int n_total, bool smem_matrix, StateBuf<D> b,
-                        const uint32_t* cstart, StateBuf<D> a, uint32_t* cell, uint32_t* rank, uint32_t* counts,
-                        uint32_t* defer, const DebugOut* dbg, int variant) {
+                        const uint32_t* cstart, const uint32_t* slot_cell, StateBuf<D> a, uint32_t* cell,
+                        uint32_t* counts, uint32_t* defer, const DebugOut* dbg, int variant) {
     if (n_total <= 0 || nworlds <= 0 || tiles <= 0) return;
     ForceParams none{};
-    ForceArgs<D> A = make_args<D>(none, b, cstart, a, cell, rank, counts, defer, dbg);
+    ForceArgs<D> A = make_args<D>(none, b, cstart, slot_cell, a, cell, counts, defer, dbg);
     A.worlds = worlds;
     A.wp_off = wp_off;
     A.tile_off = tile_off;
@@ -1052,16 +1155,16 @@ int tile_targets(int dim, int variant) {
 }
 
 template void launch_force_batch<2>(cudaStream_t, const ForceParams*, const int*, const int*, const int*, int, int,
-                                    int, bool, StateBuf<2>, const uint32_t*, StateBuf<2>, uint32_t*, uint32_t*,
+                                    int, bool, StateBuf<2>, const uint32_t*, const uint32_t*, StateBuf<2>, uint32_t*,
                                     uint32_t*, uint32_t*, const DebugOut*, int);
 template void launch_force_batch<3>(cudaStream_t, const ForceParams*, const int*, const int*, const int*, int, int,
-                                    int, bool, StateBuf<3>, const uint32_t*, StateBuf<3>, uint32_t*, uint32_t*,
+                                    int, bool, StateBuf<3>, const uint32_t*, const uint32_t*, StateBuf<3>, uint32_t*,
                                     uint32_t*, uint32_t*, const DebugOut*, int);
 
-template void launch_force<2>(cudaStream_t, const ForceParams&, bool, StateBuf<2>, const uint32_t*, StateBuf<2>,
-                              uint32_t*, uint32_t*, uint32_t*, uint32_t*, const DebugOut*, int);
-template void launch_force<3>(cudaStream_t, const ForceParams&, bool, StateBuf<3>, const uint32_t*, StateBuf<3>,
-                              uint32_t*, uint32_t*, uint32_t*, uint32_t*, const DebugOut*, int);
+template void launch_force<2>(cudaStream_t, const ForceParams&, bool, StateBuf<2>, const uint32_t*, const uint32_t*,
+                              StateBuf<2>, uint32_t*, uint32_t*, uint32_t*, const DebugOut*, int);
+template void launch_force<3>(cudaStream_t, const ForceParams&, bool, StateBuf<3>, const uint32_t*, const uint32_t*,
+                              StateBuf<3>, uint32_t*, uint32_t*, uint32_t*, const DebugOut*, int);
 
 template <int D, bool DBG, bool SMEM_M, bool BATCH, int V>
 cudaError_t allow_one() {

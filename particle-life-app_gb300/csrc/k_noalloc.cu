@@ -19,9 +19,9 @@
 //
 // Scratch contents (32-bit words), all sized for the stated maxima:
 //   cell[kMaxParticles]   cell of each particle
-//   rank[kMaxParticles]   rank inside its cell in atomic (unstable) order
 //   tmp[kMaxParticles]    unstable cell-sorted order
-//   counts[kMaxCells]     per-cell counts; must be zero before counting
+//   counts[kMaxCells]     per-cell counts; must be zero before counting (the
+//                         scatter drains them back to zero)
 //   own status word       used when the caller passes no status word
 //   scan tile words       (64-bit) look-back state; must be zero before the scan
 // Every call zeroes counts and the scan words itself (cudaMemsetAsync on the
@@ -39,9 +39,8 @@ namespace {
 constexpr int kThreads = 256;
 constexpr int64_t kMaxParticles = PLG_NOALLOC_MAX_PARTICLES;
 constexpr int64_t kMaxCells = PLG_NOALLOC_MAX_CELLS;
-constexpr int64_t kOffRank = kMaxParticles;
-constexpr int64_t kOffTmp = 2 * kMaxParticles;
-constexpr int64_t kOffCounts = 3 * kMaxParticles;
+constexpr int64_t kOffTmp = kMaxParticles;
+constexpr int64_t kOffCounts = 2 * kMaxParticles;
 constexpr int64_t kOffStatus = kOffCounts + kMaxCells;
 constexpr int64_t kOffScan = kOffStatus + 64;        // 256-byte aligned, 64-bit words from here
 constexpr int64_t kScanWords = kMaxCells / 256 + 2;  // enough for scan tiles of >= 256 cells
@@ -72,8 +71,8 @@ __device__ __forceinline__ int axis_cell_f64(double x, double cs, int nx, uint32
 
 template <int D>
 __global__ void __launch_bounds__(kThreads) k_bin_f64(int n, const double* __restrict__ pos, double cs, int nx,
-                                                      uint32_t* __restrict__ cell, uint32_t* __restrict__ rank,
-                                                      uint32_t* counts, uint32_t* status) {
+                                                      uint32_t* __restrict__ cell, uint32_t* counts,
+                                                      uint32_t* status) {
     const int i = blockIdx.x * kThreads + threadIdx.x;
     const bool valid = i < n;
     uint32_t c = 0;
@@ -89,7 +88,7 @@ __global__ void __launch_bounds__(kThreads) k_bin_f64(int n, const double* __res
     }
     const unsigned mask = __ballot_sync(kFull, valid);
     if (valid) {
-        rank[i] = bin_count(counts, c, mask);
+        bin_add(counts, c, mask);
         cell[i] = c;
     }
 }
@@ -172,7 +171,6 @@ extern "C" int plg_sort_cells_noalloc(int32_t dim, double rmax, int64_t n, const
         return PLG_E_CUDA;
     }
     uint32_t* cell = scratch;
-    uint32_t* rank = scratch + kOffRank;
     uint32_t* tmp = scratch + kOffTmp;
     uint32_t* counts = scratch + kOffCounts;
     uint32_t* st_word = status ? status : scratch + kOffStatus;
@@ -190,14 +188,14 @@ extern "C" int plg_sort_cells_noalloc(int32_t dim, double rmax, int64_t n, const
     const double cs = rmax;  // containerSize = settings.rmax (Physics.java:312)
     if (ni > 0) {
         if (dim == 2) {
-            k_bin_f64<2><<<blocks, kThreads, 0, s>>>(ni, pos, cs, nx, cell, rank, counts, st_word);
+            k_bin_f64<2><<<blocks, kThreads, 0, s>>>(ni, pos, cs, nx, cell, counts, st_word);
         } else {
-            k_bin_f64<3><<<blocks, kThreads, 0, s>>>(ni, pos, cs, nx, cell, rank, counts, st_word);
+            k_bin_f64<3><<<blocks, kThreads, 0, s>>>(ni, pos, cs, nx, cell, counts, st_word);
         }
     }
     launch_scan(s, counts, (int)ncells, cell_start, scan_state, st_word, nullptr);
     if (ni > 0) {
-        launch_scatter(s, ni, cell, rank, cell_start, tmp);
+        launch_scatter(s, ni, cell, counts, cell_start, tmp);
         k_stable_order<<<blocks, kThreads, 0, s>>>(ni, tmp, cell, cell_start, perm);
     }
     if (cudaGetLastError() != cudaSuccess) return PLG_E_CUDA;

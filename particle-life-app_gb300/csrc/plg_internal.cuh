@@ -91,16 +91,26 @@ __device__ __forceinline__ uint32_t cell_index(float x, float y, float z, const 
 }
 
 // Counting step of makeContainers (Physics.java:328-332) for one particle per
-// lane: lanes of a warp with the same cell add once, and each lane's rank in
-// its cell follows lane order.  `mask` = lanes taking part (all must call).
-__device__ __forceinline__ uint32_t bin_count(uint32_t* counts, uint32_t cell, unsigned mask) {
+// lane: lanes of a warp with the same cell add once, without waiting for the
+// result.  `mask` = lanes taking part (all must call).
+__device__ __forceinline__ void bin_add(uint32_t* counts, uint32_t cell, unsigned mask) {
+    const unsigned peers = __match_any_sync(mask, cell);
+    if ((threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(counts + cell, (uint32_t)__popc(peers));
+}
+
+// A rank in [0, counts[cell]) for one particle per lane, distinct for every
+// caller of the cell; counts[cell] goes back down to 0 once every member
+// has taken one.  The order of the ranks is arbitrary (the gather re-ranks
+// the members stably).
+__device__ __forceinline__ uint32_t bin_take(uint32_t* counts, uint32_t cell, unsigned mask) {
     const unsigned peers = __match_any_sync(mask, cell);
     const int lane = threadIdx.x & 31;
     const int leader = __ffs(peers) - 1;
-    uint32_t base = 0;
-    if (lane == leader) base = atomicAdd(counts + cell, (uint32_t)__popc(peers));
-    base = __shfl_sync(peers, base, leader);
-    return base + (uint32_t)__popc(peers & ((1u << lane) - 1u));
+    const uint32_t k = (uint32_t)__popc(peers);
+    uint32_t top = 0;
+    if (lane == leader) top = atomicSub(counts + cell, k);
+    top = __shfl_sync(peers, top, leader);
+    return top - k + (uint32_t)__popc(peers & ((1u << lane) - 1u));
 }
 
 // splitmix64 output function (Steele, Lea, Flood 2014) on id + gamma: the
@@ -169,8 +179,8 @@ struct StateBuf {
 // id_base: the id of the first particle (ids are id_base + index).
 template <int D>
 void launch_upload(cudaStream_t st, int n, const double* pos, const double* vel, const int32_t* type,
-                   int ntypes, StateBuf<D> a, uint32_t* cell, uint32_t* rank, uint32_t* counts, Grid g,
-                   uint32_t* status, uint32_t cell_base = 0, int id_base = 0);
+                   int ntypes, StateBuf<D> a, uint32_t* cell, uint32_t* counts, Grid g, uint32_t* status,
+                   uint32_t cell_base = 0, int id_base = 0);
 
 // ---- initialisers (k_init.cu) ----
 // Position setters (app/PositionSetterProvider.java), type setters
@@ -247,11 +257,10 @@ void launch_batch_move(cudaStream_t st, int n, const int* new_off, const int* ol
 // world's grid (worlds[k].cell_base + cell), for the next sort.
 template <int D>
 void launch_batch_rebin(cudaStream_t st, int n, StateBuf<D> a, const ForceParams* worlds, const int* wp_off, int nw,
-                        uint32_t* cell, uint32_t* rank, uint32_t* counts);
+                        uint32_t* cell, uint32_t* counts);
 
 template <int D>
-void launch_rebin(cudaStream_t st, int n, StateBuf<D> a, uint32_t* cell, uint32_t* rank, uint32_t* counts,
-                  Grid g);
+void launch_rebin(cudaStream_t st, int n, StateBuf<D> a, uint32_t* cell, uint32_t* counts, Grid g);
 
 template <int D>
 void launch_download(cudaStream_t st, int n, StateBuf<D> a, double* pos, double* vel, int32_t* type,
@@ -260,22 +269,25 @@ void launch_download(cudaStream_t st, int n, StateBuf<D> a, double* pos, double*
 int scan_blocks(int ncells);
 // state: (scan_blocks + 1) words, zeroed before each launch; *zero_word is
 // set to 0 (the step's deferred-target count) when not null.
-void launch_scan(cudaStream_t st, uint32_t* counts, int ncells, uint32_t* cstart, unsigned long long* state,
+void launch_scan(cudaStream_t st, const uint32_t* counts, int ncells, uint32_t* cstart, unsigned long long* state,
                  uint32_t* status, uint32_t* zero_word);
+// perm[cstart[cell[i]] + r] = i with a rank r taken from counts[cell[i]]
+// (bin_take), which leaves counts at zero for the next counting pass.
 // slot_cell (may be null): receives the cell of each sorted slot.
-void launch_scatter(cudaStream_t st, int n, const uint32_t* cell, const uint32_t* rank, const uint32_t* cstart,
+void launch_scatter(cudaStream_t st, int n, const uint32_t* cell, uint32_t* counts, const uint32_t* cstart,
                     uint32_t* perm, uint32_t* slot_cell = nullptr);
 
 template <int D>
 void launch_gather(cudaStream_t st, int n, const uint32_t* perm, const uint32_t* slot_cell, const uint32_t* cstart,
                    StateBuf<D> a, StateBuf<D> b, int32_t* cell_sorted);
 
+// slot_cell: the cell of each slot of b, as the scatter wrote it.
 // `defer`: one word, zeroed before the step; counts the targets the tiled
 // kernel recomputed in its deferred pass.
 // variant: tile variant of the force kernel (0 or 1, the autotuner's knob).
 template <int D>
 void launch_force(cudaStream_t st, const ForceParams& p, bool general, StateBuf<D> b, const uint32_t* cstart,
-                  StateBuf<D> a, uint32_t* cell, uint32_t* rank, uint32_t* counts, uint32_t* defer,
+                  const uint32_t* slot_cell, StateBuf<D> a, uint32_t* cell, uint32_t* counts, uint32_t* defer,
                   const DebugOut* dbg, int variant = 0);
 
 // Batched worlds: `worlds` (device, nworlds entries) holds each world's
@@ -289,8 +301,8 @@ void launch_force(cudaStream_t st, const ForceParams& p, bool general, StateBuf<
 template <int D>
 void launch_force_batch(cudaStream_t st, const ForceParams* worlds, const int* wp_off, const int* tile_off,
                         const int* steps_left, int tiles, int nworlds, int n_total, bool smem_matrix, StateBuf<D> b,
-                        const uint32_t* cstart, StateBuf<D> a, uint32_t* cell, uint32_t* rank, uint32_t* counts,
-                        uint32_t* defer, const DebugOut* dbg, int variant = 0);
+                        const uint32_t* cstart, const uint32_t* slot_cell, StateBuf<D> a, uint32_t* cell,
+                        uint32_t* counts, uint32_t* defer, const DebugOut* dbg, int variant = 0);
 
 // Counts every positive steps_left[k] (k < nworlds) down by one.
 void launch_batch_tick(cudaStream_t st, int* steps_left, int nworlds);

@@ -118,7 +118,7 @@ struct plg_ctx {
     bool have_settings = false;
     bool have_matrix = false;
     bool state_valid = false;  // an upload succeeded
-    bool bins_dirty = false;   // cell/rank/counts must be recomputed from A
+    bool bins_dirty = false;   // cell/counts must be recomputed from A
 
     // grid
     int nx = 0;
@@ -145,7 +145,6 @@ struct plg_ctx {
     void* avel = nullptr;
     void* bvel = nullptr;
     uint32_t* cell = nullptr;
-    uint32_t* rank = nullptr;
     uint32_t* perm = nullptr;
     uint32_t* slot_cell = nullptr;  // cell of each sorted slot (scatter -> gather)
     uint32_t* defer = nullptr;  // targets the force kernel deferred in the last step
@@ -280,13 +279,13 @@ void enqueue_body(plg_ctx* c, const DebugOut* dbg, int32_t* cell_sorted) {
     launch_scan(st, c->counts, c->ncells, c->cstart, c->scan_state, c->status_d, c->general ? nullptr : c->defer);
     k1(PLG_K_SCAN);
     k0(PLG_K_SCATTER);
-    launch_scatter(st, n, c->cell, c->rank, c->cstart, c->perm, c->slot_cell);
+    launch_scatter(st, n, c->cell, c->counts, c->cstart, c->perm, c->slot_cell);
     k1(PLG_K_SCATTER);
     k0(PLG_K_GATHER);
     launch_gather<D>(st, n, c->perm, c->slot_cell, c->cstart, buf_a<D>(c), buf_b<D>(c), cell_sorted);
     k1(PLG_K_GATHER);
     k0(PLG_K_FORCE);
-    launch_force<D>(st, c->fp, c->general, buf_b<D>(c), c->cstart, buf_a<D>(c), c->cell, c->rank, c->counts,
+    launch_force<D>(st, c->fp, c->general, buf_b<D>(c), c->cstart, c->slot_cell, buf_a<D>(c), c->cell, c->counts,
                     c->defer, dbg);
     k1(PLG_K_FORCE);
 }
@@ -302,9 +301,9 @@ int enqueue_rebin(plg_ctx* c) {
     if (!c->bins_dirty) return PLG_OK;
     CK(c, cudaMemsetAsync(c->counts, 0, sizeof(uint32_t) * (size_t)c->ncells, c->stream));
     if (c->dim == 2)
-        launch_rebin<2>(c->stream, (int)c->n, buf_a<2>(c), c->cell, c->rank, c->counts, grid_of(c));
+        launch_rebin<2>(c->stream, (int)c->n, buf_a<2>(c), c->cell, c->counts, grid_of(c));
     else
-        launch_rebin<3>(c->stream, (int)c->n, buf_a<3>(c), c->cell, c->rank, c->counts, grid_of(c));
+        launch_rebin<3>(c->stream, (int)c->n, buf_a<3>(c), c->cell, c->counts, grid_of(c));
     CK(c, cudaGetLastError());
     c->bins_dirty = false;
     return PLG_OK;
@@ -396,7 +395,7 @@ int read_status(plg_ctx* c) {
 int free_all(plg_ctx* c) {
     destroy_graph(c);
     void* ptrs[] = {c->bounds,    c->counts,   c->cstart,   c->scan_state, c->matrix,   c->apt,
-                    c->bpt,       c->avel,     c->bvel,     c->cell,       c->rank,     c->perm,
+                    c->bpt,       c->avel,     c->bvel,     c->cell,       c->perm,
                     c->slot_cell, c->defer,    c->stage,    c->status_d,   c->dbg_pairs, c->dbg_hsum,
                     c->dbg_hxor,  c->dbg_cand, c->dbg_acc,  c->dbg_cell, c->edit_flag, c->edit_off,
                     c->edit_scan, c->edit_cnt};
@@ -497,7 +496,6 @@ int plg_create(int dim, int64_t capacity, plg_ctx** out) {
     dmalloc(&c->avel, vel_sz * cap);
     dmalloc(&c->bvel, vel_sz * cap);
     dmalloc((void**)&c->cell, sizeof(uint32_t) * cap);
-    dmalloc((void**)&c->rank, sizeof(uint32_t) * cap);
     dmalloc((void**)&c->perm, sizeof(uint32_t) * cap);
     dmalloc((void**)&c->slot_cell, sizeof(uint32_t) * cap);
     dmalloc((void**)&c->defer, sizeof(uint32_t));
@@ -631,11 +629,11 @@ int plg_upload(plg_ctx* c, int64_t n, const double* pos, const double* vel, cons
     CK(c, cudaMemsetAsync(c->counts, 0, sizeof(uint32_t) * (size_t)c->ncells, st));
     CK(c, cudaMemsetAsync(c->status_d, 0, sizeof(uint32_t), st));
     if (c->dim == 2)
-        launch_upload<2>(st, (int)n, dpos, vel ? dvel : nullptr, dtype, c->ntypes, buf_a<2>(c), c->cell, c->rank,
-                         c->counts, grid_of(c), c->status_d);
+        launch_upload<2>(st, (int)n, dpos, vel ? dvel : nullptr, dtype, c->ntypes, buf_a<2>(c), c->cell, c->counts,
+                         grid_of(c), c->status_d);
     else
-        launch_upload<3>(st, (int)n, dpos, vel ? dvel : nullptr, dtype, c->ntypes, buf_a<3>(c), c->cell, c->rank,
-                         c->counts, grid_of(c), c->status_d);
+        launch_upload<3>(st, (int)n, dpos, vel ? dvel : nullptr, dtype, c->ntypes, buf_a<3>(c), c->cell, c->counts,
+                         grid_of(c), c->status_d);
     CK(c, cudaGetLastError());
     int rc = read_status(c);
     if (rc) return rc;
@@ -901,12 +899,12 @@ int plg_append(plg_ctx* c, int64_t n, const double* pos, const double* vel, cons
     const int64_t off = c->n;
     if (c->dim == 2)
         launch_upload<2>(st, (int)n, dpos, vel ? dvel : nullptr, dtype, c->ntypes,
-                         StateBuf<2>{c->apt + off, (float2*)c->avel + off}, c->cell + off, c->rank + off, c->counts,
-                         grid_of(c), c->status_d, 0, (int)c->next_id);
+                         StateBuf<2>{c->apt + off, (float2*)c->avel + off}, c->cell + off, c->counts, grid_of(c),
+                         c->status_d, 0, (int)c->next_id);
     else
         launch_upload<3>(st, (int)n, dpos, vel ? dvel : nullptr, dtype, c->ntypes,
-                         StateBuf<3>{c->apt + off, (float4*)c->avel + off}, c->cell + off, c->rank + off, c->counts,
-                         grid_of(c), c->status_d, 0, (int)c->next_id);
+                         StateBuf<3>{c->apt + off, (float4*)c->avel + off}, c->cell + off, c->counts, grid_of(c),
+                         c->status_d, 0, (int)c->next_id);
     CK(c, cudaGetLastError());
     if ((rc = read_status(c))) return rc;
     c->next_id += n;
