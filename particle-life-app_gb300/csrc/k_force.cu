@@ -318,12 +318,13 @@ __device__ __forceinline__ bool stage_columns(const ForceArgs<D>& A, const Force
 
 
 // Main force kernel (nx >= 3): one thread per target; a block takes 256 (3D:
-// 128) consecutive targets and, per segment (targets of one grid row), stages
-// the segment's stencil so that each target reads one contiguous run (or,
-// when the segment does not fit, reads the same cells from global memory).
-// FP32 only: a target whose neighbourhood holds a candidate that needs the
-// FP64 decision is deferred to the block's closing pass (fixup_target), which
-// recomputes it completely.
+// 128) consecutive targets, stages their windows so that each target reads
+// one contiguous run (or, where a window does not fit, reads the same cells
+// from global memory).  Neighbouring threads mostly share a cell, hence a
+// window, so their candidate loads are broadcasts.  FP32 only: a target
+// whose neighbourhood holds a candidate that needs the FP64 decision is
+// deferred to its warp's closing pass (fixup_target), which recomputes it
+// completely.
 // BATCH: the sorted order holds many worlds one after another (their cells
 // are disjoint ranges of one global cell index).  Tiles are laid out per
 // world: block b works on tile b - tile_off[k] of the world k that owns it,
@@ -454,12 +455,14 @@ __global__ void __launch_bounds__(TileCfg<D, V>::kTargets, TileCfg<D, V>::kMinBl
         const int own = (k + 1) * R + R / 2;
         const int self_j = sm.coff[own] + (s - sm.cglob[own]);
         const bool shift = P.wrap && (cx == nx - 1 || cy == nx - 1 || (D == 3 && cz == nx - 1));
+        const int* co = sm.coff;
+        const int* cg = sm.cglob;
         if (shift) {
-            defer = cand_range<D, DBG, true>(A, P, sm.cand, sm.coff, sm.cglob, Mrow, ncell, j0, self_j, px, py, pz, acc);
-            defer |= cand_range<D, DBG, true>(A, P, sm.cand, sm.coff, sm.cglob, Mrow, ncell, self_j + 1, j1, px, py, pz, acc);
+            defer = cand_range<D, DBG, true>(A, P, sm.cand, co, cg, Mrow, ncell, j0, self_j, px, py, pz, acc);
+            defer |= cand_range<D, DBG, true>(A, P, sm.cand, co, cg, Mrow, ncell, self_j + 1, j1, px, py, pz, acc);
         } else {
-            defer = cand_range<D, DBG, false>(A, P, sm.cand, sm.coff, sm.cglob, Mrow, ncell, j0, self_j, px, py, pz, acc);
-            defer |= cand_range<D, DBG, false>(A, P, sm.cand, sm.coff, sm.cglob, Mrow, ncell, self_j + 1, j1, px, py, pz, acc);
+            defer = cand_range<D, DBG, false>(A, P, sm.cand, co, cg, Mrow, ncell, j0, self_j, px, py, pz, acc);
+            defer |= cand_range<D, DBG, false>(A, P, sm.cand, co, cg, Mrow, ncell, self_j + 1, j1, px, py, pz, acc);
         }
     };
     __syncthreads();
