@@ -32,6 +32,7 @@ from __future__ import annotations
 import argparse
 import json
 import os
+import re
 import subprocess
 import sys
 import tempfile
@@ -48,11 +49,14 @@ METRIC = "particle-steps/s at 1M 2D"
 UNIT = "particle-steps/s"
 FRICTION = 0.5 ** (1.0 / (60.0 * 0.043))
 
-# Algorithmic work per unit (FMA = 2 flops; compare and rsqrt = 1).
-FLOPS_PER_CANDIDATE = {2: 6, 3: 9}
-FLOPS_PER_INTERACTION = {2: 13, 3: 15}
-# Bytes each kernel must move per particle / per cell, by design (2D layout).
-BYTES = {"scatter": 12, "gather": 56, "force": 56, "scan_cell": 12}
+# Algorithmic work per unit, as include/plg_work.h fixes it (FMA = 2 flops;
+# compare and rsqrt = 1; bytes by design, 2D layout).
+WORK = {m.group(1): int(m.group(2)) for m in
+        re.finditer(r"^#define (PLG_WORK_\w+) (\d+)", (REPO / "include" / "plg_work.h").read_text(), re.M)}
+FLOPS_PER_CANDIDATE = {2: WORK["PLG_WORK_FLOPS_CANDIDATE_2D"], 3: WORK["PLG_WORK_FLOPS_CANDIDATE_3D"]}
+FLOPS_PER_INTERACTION = {2: WORK["PLG_WORK_FLOPS_INTERACTION_2D"], 3: WORK["PLG_WORK_FLOPS_INTERACTION_3D"]}
+BYTES = {"scatter": WORK["PLG_WORK_SCATTER_BYTES"], "gather": WORK["PLG_WORK_GATHER_BYTES_2D"],
+         "force": WORK["PLG_WORK_FORCE_BYTES_2D"], "scan_cell": WORK["PLG_WORK_SCAN_BYTES_PER_CELL"]}
 
 
 def parse():
@@ -465,7 +469,6 @@ def run_ours(args):
     traffic = None
     tf = REPO / "profiles" / "k_force_tile_2d_1m.md"  # ncu summary of this kernel on this workload
     if tf.exists():
-        import re
 
         mt = re.search(r"^dram_bytes_per_launch: (\d+)", tf.read_text(), re.M)
         traffic = int(mt.group(1)) if mt else None
