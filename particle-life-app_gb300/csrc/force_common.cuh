@@ -364,20 +364,31 @@ __device__ __forceinline__ float rsqrt_approx(float x) {
 // Loop constants of the candidate evaluation, read once into registers
 // (otherwise the compiler re-reads them from the parameter bank per
 // candidate).
+// The decision band as |d2 - mid| < half: lo, mid and hi are floats a few
+// ulp apart, so hi - lo, mid - lo and hi - mid are exact, mid lies in
+// [lo, hi], and (mid - half, mid + half) contains (lo, hi); for d2 within a
+// factor 2 of mid the subtraction d2 - mid is exact too, and any other d2 is
+// far outside.  brm2 = (beta rmax)^2: the repulsion branch tests d2, which
+// is ready before the rsqrt.
 struct LoopK {
-    float lo, hi, tiny, m2, opb, iomb, brm, k1;
+    float lo, hi, tiny, m2, opb, iomb, k1, brm2, mid, half;
     __device__ __forceinline__ explicit LoopK(const ForceParams& P)
         : lo(P.lo), hi(P.hi), tiny(P.tiny), m2(P.m2_inv_rmax), opb(P.one_plus_beta),
-          iomb(P.inv_one_minus_beta), brm(P.beta_rmax), k1(P.k1) {}
+          iomb(P.inv_one_minus_beta), k1(P.k1), brm2(P.beta_rmax * P.beta_rmax) {
+        mid = lo + (hi - lo) * 0.5f;
+        half = fmaxf(mid - lo, hi - mid);
+    }
 };
 
 // One candidate: d = q - p with the image shifts already applied to q and p,
-// the FP32 Accelerator term added to acc, band / tiny pairs flagged in rare.
+// the FP32 Accelerator term added to acc; bmin / dmin keep the smallest
+// |d2 - mid| and d2 seen, from which the caller flags band and tiny pairs
+// (a running minimum costs fewer instructions than a flag per candidate).
 // The staged and the direct paths both use it, in the same candidate order,
 // so they produce the same bits.  Returns d2.
 template <int D>
 __device__ __forceinline__ float eval_candidate(const LoopK& K, float qx, float qy, float qz, float pxe, float pye,
-                                                float pze, float a, Acc& acc, bool& rare) {
+                                                float pze, float a, Acc& acc, float& bmin, float& dmin) {
     const float dx = qx - pxe;
     const float dy = qy - pye;
     float d2;
@@ -388,12 +399,13 @@ __device__ __forceinline__ float eval_candidate(const LoopK& K, float qx, float 
     } else {
         d2 = fmaf(dx, dx, dy * dy);
     }
-    rare |= ((d2 > K.lo) & (d2 < K.hi)) | (d2 < K.tiny);
+    bmin = fminf(bmin, fabsf(d2 - K.mid));
+    dmin = fminf(dmin, d2);
     const float inv = rsqrt_approx(d2);
     const float dist = d2 * inv;
     const float t = fmaf(dist, K.m2, K.opb);
     const float u = fmaxf(fmaf(-fabsf(t), K.iomb, 1.f), 0.f);
-    const float g = dist < K.brm ? K.k1 - inv : (a * inv) * u;
+    const float g = d2 < K.brm2 ? K.k1 - inv : (a * inv) * u;
     acc.x = fmaf(dx, g, acc.x);
     acc.y = fmaf(dy, g, acc.y);
     if (D == 3) acc.z = fmaf(dz, g, acc.z);
@@ -429,7 +441,7 @@ __device__ __forceinline__ bool cand_range(const ForceArgs<D>& A, const ForcePar
                                            const int* coff, const int* cglob, const float* __restrict__ Mrow,
                                            int ncell, int ja, int jb, float px, float py, float pz, Acc& acc) {
     const float px1 = px - 1.f, py1 = py - 1.f, pz1 = pz - 1.f;
-    bool rare = false;
+    float bmin = INFINITY, dmin = INFINITY;
     const LoopK K(P);
     for (int j = ja; j < jb; ++j) {
         const float4 q = cand[j];
@@ -441,7 +453,7 @@ __device__ __forceinline__ bool cand_range(const ForceArgs<D>& A, const ForcePar
             if (D == 3) pze = (tb & kShiftZ) ? pz1 : pz;
             tb &= 0xffff;
         }
-        const float d2 = eval_candidate<D>(K, q.x, q.y, q.z, pxe, pye, pze, Mrow[tb], acc, rare);
+        const float d2 = eval_candidate<D>(K, q.x, q.y, q.z, pxe, pye, pze, Mrow[tb], acc, bmin, dmin);
         if (DBG) {
             acc.cand++;
             if ((d2 <= K.lo) & (d2 >= K.tiny))
@@ -449,7 +461,7 @@ __device__ __forceinline__ bool cand_range(const ForceArgs<D>& A, const ForcePar
                                   id_of<D>(A, staged_global(coff, cglob, ncell, j)));
         }
     }
-    return rare;
+    return (bmin < K.half) | (dmin < K.tiny);
 }
 
 // The target's neighbourhood read straight from global memory, for segments
@@ -466,7 +478,7 @@ __device__ __noinline__ bool direct_stencil(const ForceArgs<D>& A, const ForcePa
     const LoopK K(P);
     const int nx = P.g.nx;
     const bool wrap = P.wrap != 0;
-    bool rare = false;
+    float bmin = INFINITY, dmin = INFINITY;
     for (int ci = 0; ci < 3; ++ci) {
         int col = cx - 1 + ci;
         bool qsx = false, tsx = false;
@@ -507,7 +519,7 @@ __device__ __noinline__ bool direct_stencil(const ForceArgs<D>& A, const ForcePa
                 if (qsy) q.y -= 1.f;
                 if (D == 3 && qsz) q.z -= 1.f;
                 const float d2 = eval_candidate<D>(K, q.x, q.y, q.z, pxe, pye, pze, Mrow[Layout<D>::type(q)], acc,
-                                                   rare);
+                                                   bmin, dmin);
                 if (DBG) {
                     acc.cand++;
                     if ((d2 <= K.lo) & (d2 >= K.tiny))
@@ -516,7 +528,7 @@ __device__ __noinline__ bool direct_stencil(const ForceArgs<D>& A, const ForcePa
             }
         }
     }
-    return rare;
+    return (bmin < K.half) | (dmin < K.tiny);
 }
 
 // Sum of `v` over the warp in a fixed butterfly order (the same bits on
