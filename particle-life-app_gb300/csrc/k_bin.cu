@@ -22,7 +22,7 @@ namespace {
 
 constexpr int kThreads = 256;
 constexpr int kScanThreads = 256;
-constexpr int kScanItems = 4;
+constexpr int kScanItems = 16;
 constexpr int kScanTile = kScanThreads * kScanItems;
 
 inline int blocks_for(int n, int threads) { return (n + threads - 1) / threads; }
@@ -274,11 +274,14 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(const uint32_t* __restric
     const int base = tile * kScanTile + threadIdx.x * kScanItems;
     uint32_t v[kScanItems];
     if (base + kScanItems <= ncells) {
-        const uint4 q = *reinterpret_cast<const uint4*>(counts + base);
-        v[0] = q.x;
-        v[1] = q.y;
-        v[2] = q.z;
-        v[3] = q.w;
+#pragma unroll
+        for (int q4 = 0; q4 < kScanItems / 4; ++q4) {
+            const uint4 q = *reinterpret_cast<const uint4*>(counts + base + 4 * q4);
+            v[4 * q4] = q.x;
+            v[4 * q4 + 1] = q.y;
+            v[4 * q4 + 2] = q.z;
+            v[4 * q4 + 3] = q.w;
+        }
     } else {
 #pragma unroll
         for (int k = 0; k < kScanItems; ++k) v[k] = base + k < ncells ? counts[base + k] : 0u;
@@ -326,13 +329,17 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(const uint32_t* __restric
     __syncthreads();
     uint32_t run = s_prefix + ex;
     if (base + kScanItems <= ncells) {
-        uint4 o;
-        o.x = run;
-        o.y = run + v[0];
-        o.z = o.y + v[1];
-        o.w = o.z + v[2];
-        *reinterpret_cast<uint4*>(cstart + base) = o;
-        if (base + kScanItems == ncells) cstart[ncells] = o.w + v[3];
+#pragma unroll
+        for (int q4 = 0; q4 < kScanItems / 4; ++q4) {
+            uint4 o;
+            o.x = run;
+            o.y = o.x + v[4 * q4];
+            o.z = o.y + v[4 * q4 + 1];
+            o.w = o.z + v[4 * q4 + 2];
+            run = o.w + v[4 * q4 + 3];
+            *reinterpret_cast<uint4*>(cstart + base + 4 * q4) = o;
+        }
+        if (base + kScanItems == ncells) cstart[ncells] = run;
     } else {
 #pragma unroll
         for (int k = 0; k < kScanItems; ++k) {
@@ -347,18 +354,43 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(const uint32_t* __restric
 }
 
 // Each particle takes a slot of its cell (the ranks drain counts back to
-// zero for the next counting pass).
+// zero for the next counting pass).  kScatterPer particles per thread, their
+// atomics in flight together.
+constexpr int kScatterPer = 4;
 __global__ void __launch_bounds__(kThreads) k_scatter(int n, const uint32_t* __restrict__ cell, uint32_t* counts,
                                                       const uint32_t* __restrict__ cstart,
                                                       uint32_t* __restrict__ perm, uint32_t* __restrict__ slot_cell) {
-    const int i = blockIdx.x * kThreads + threadIdx.x;
-    const bool valid = i < n;
-    const uint32_t c = valid ? cell[i] : 0u;
-    const unsigned mask = __ballot_sync(kFull, valid);
-    if (!valid) return;
-    const uint32_t slot = __ldg(cstart + c) + bin_take(counts, c, mask);
-    perm[slot] = (uint32_t)i;
-    if (slot_cell) slot_cell[slot] = c;
+    const int i0 = blockIdx.x * (kThreads * kScatterPer) + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    uint32_t c[kScatterPer], top[kScatterPer];
+    unsigned peers[kScatterPer];
+    bool v[kScatterPer];
+#pragma unroll
+    for (int k = 0; k < kScatterPer; ++k) {
+        const int i = i0 + k * kThreads;
+        v[k] = i < n;
+        c[k] = v[k] ? cell[i] : 0u;
+    }
+#pragma unroll
+    for (int k = 0; k < kScatterPer; ++k) {
+        const unsigned m = __ballot_sync(kFull, v[k]);
+        peers[k] = 0u;
+        top[k] = 0u;
+        if (v[k]) {
+            peers[k] = __match_any_sync(m, c[k]);
+            if (lane == __ffs(peers[k]) - 1) top[k] = atomicSub(counts + c[k], (uint32_t)__popc(peers[k]));
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < kScatterPer; ++k) {
+        if (!v[k]) continue;
+        const unsigned pk = peers[k];
+        const uint32_t t = __shfl_sync(pk, top[k], __ffs(pk) - 1);
+        const uint32_t r = t - (uint32_t)__popc(pk) + (uint32_t)__popc(pk & ((1u << lane) - 1u));
+        const uint32_t slot = __ldg(cstart + c[k]) + r;
+        perm[slot] = (uint32_t)(i0 + k * kThreads);
+        if (slot_cell) slot_cell[slot] = c[k];
+    }
 }
 
 // Places particle i = perm[s] at its rank among its cell's members by
@@ -448,7 +480,7 @@ void launch_scan(cudaStream_t st, const uint32_t* counts, int ncells, uint32_t* 
 void launch_scatter(cudaStream_t st, int n, const uint32_t* cell, uint32_t* counts, const uint32_t* cstart,
                     uint32_t* perm, uint32_t* slot_cell) {
     if (n <= 0) return;
-    k_scatter<<<blocks_for(n, kThreads), kThreads, 0, st>>>(n, cell, counts, cstart, perm, slot_cell);
+    k_scatter<<<blocks_for(n, kThreads * kScatterPer), kThreads, 0, st>>>(n, cell, counts, cstart, perm, slot_cell);
 }
 
 template <int D>
