@@ -42,6 +42,16 @@ namespace {
 constexpr int kThreads = 256;        // literal-path and fixup kernels
 constexpr int kSmemMatrixMax = 16;   // matrix in shared memory up to 16 x 16
 
+// Row stride of the matrix in shared memory.  3D: odd, so that the lanes of
+// a warp reading one column from different rows (targets of different types
+// against one candidate) hit distinct banks (16 types with stride 16 put a
+// column in two banks: 3D blobs ran 3% slower).  2D: the plain stride (at
+// most 2-way conflicts for 8 types; the padded form measured 1% slower).
+template <int D>
+__host__ __device__ constexpr int smem_matrix_stride(int ntypes) {
+    return D == 3 ? (ntypes | 1) : ntypes;
+}
+
 
 
 struct Acc {
@@ -542,12 +552,14 @@ __device__ __forceinline__ float warp_sum(float v) {
 // One deferred target, one warp: the lanes split the candidates of the
 // global-memory stencil (with the FP64 decisions), their partial sums are
 // combined by warp_sum, and lane 0 runs the epilogue and the counting step.
+// M: the matrix in global memory (P.matrix) or its shared-memory copy.
 template <int D, bool DBG>
 __device__ __noinline__ void fixup_target(const ForceArgs<D>& A, const ForceParams& P, const uint32_t* cs,
                                           const float* M, int s, int lane) {
+    const int mstride = M == P.matrix ? P.ntypes : smem_matrix_stride<D>(P.ntypes);
     const float4 me = A.bpt[s];
     const float px = me.x, py = me.y, pz = D == 3 ? me.z : 0.f;
-    Acc acc = warp_stencil<D, DBG>(A, P, cs, M + Layout<D>::type(me) * P.ntypes, s, px, py, pz,
+    Acc acc = warp_stencil<D, DBG>(A, P, cs, M + Layout<D>::type(me) * mstride, s, px, py, pz,
                                    sliver_mask<D>(P, px, py, pz), lane);
     acc.x = warp_sum(acc.x);
     acc.y = warp_sum(acc.y);

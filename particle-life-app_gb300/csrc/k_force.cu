@@ -101,9 +101,10 @@ __global__ void __launch_bounds__(kThreads) k_force_general(const __grid_constan
     const ForceParams& P = A.p;
     extern __shared__ float smat[];
     const float* M = P.matrix;
+    const int nt = P.ntypes, ms = SMEM_M ? smem_matrix_stride<D>(nt) : nt;
     if (SMEM_M) {
-        const int nn = P.ntypes * P.ntypes;
-        for (int k = threadIdx.x; k < nn; k += kThreads) smat[k] = P.matrix[k];
+        for (int k = threadIdx.x; k < nt * nt; k += kThreads)
+            smat[D == 3 ? (k / nt) * ms + k % nt : k] = P.matrix[k];
         __syncthreads();
         M = smat;
     }
@@ -113,7 +114,7 @@ __global__ void __launch_bounds__(kThreads) k_force_general(const __grid_constan
     if (valid) {
         const float4 me = A.bpt[s];
         Acc acc = {0.f, 0.f, 0.f, 0, 0ull, 0ull, 0ull};
-        general_scan<D, DBG>(A, M + Layout<D>::type(me) * P.ntypes, s, me.x, me.y, D == 3 ? me.z : 0.f, acc);
+        general_scan<D, DBG>(A, M + Layout<D>::type(me) * ms, s, me.x, me.y, D == 3 ? me.z : 0.f, acc);
         newcell = integrate<D, DBG>(A, A.p, s, me, A.bvel[s], acc);
     }
     const unsigned mask = __ballot_sync(kFull, valid);
@@ -172,7 +173,7 @@ struct TileSmem {
     int wcol[TileCfg<D, V>::kTargets / 32];
     int nseg;
     int staged;                         // 1: the staged columns' candidates are in smem
-    float mat[kSmemMatrixMax * kSmemMatrixMax];
+    float mat[kSmemMatrixMax * smem_matrix_stride<D>(kSmemMatrixMax)];
 };
 
 // Block-wide exclusive scan of v[0..n) in place (n <= kCells); returns the total.
@@ -364,9 +365,9 @@ __global__ void __launch_bounds__(TileCfg<D, V>::kTargets, TileCfg<D, V>::kMinBl
         if (valid) bin_add(A.counts, c, m);
         return;
     }
+    const int nt = P.ntypes, ms = SMEM_M ? smem_matrix_stride<D>(nt) : nt;
     if (SMEM_M) {
-        const int nn = P.ntypes * P.ntypes;
-        for (int k = tid; k < nn; k += kT) sm.mat[k] = P.matrix[k];
+        for (int k = tid; k < nt * nt; k += kT) sm.mat[D == 3 ? (k / nt) * ms + k % nt : k] = P.matrix[k];
     }
     const float* M = SMEM_M ? sm.mat : P.matrix;
     float4 me = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -443,7 +444,7 @@ __global__ void __launch_bounds__(TileCfg<D, V>::kTargets, TileCfg<D, V>::kMinBl
     const int nx = P.g.nx;
     const int cy = D == 3 ? (valid ? row % nx : 0) : row, cz = D == 3 ? (valid ? row / nx : 0) : 0;
     const float px = me.x, py = me.y, pz = D == 3 ? me.z : 0.f;
-    const float* Mrow = M + (valid ? Layout<D>::type(me) : 0) * P.ntypes;
+    const float* Mrow = M + (valid ? Layout<D>::type(me) : 0) * ms;
     Acc acc = {0.f, 0.f, 0.f, 0, 0ull, 0ull, 0ull};
     bool defer = false, direct = false;
     // The target's window: staged columns k .. k+2; the target itself splits
@@ -547,7 +548,7 @@ void launch_variant(cudaStream_t st, const ForceArgs<D>& A, bool general, int va
     const bool smem = A.p.ntypes <= kSmemMatrixMax;
     if (general) {
         const int grid = (n + kThreads - 1) / kThreads;
-        const size_t sb = smem ? sizeof(float) * A.p.ntypes * A.p.ntypes : 0;
+        const size_t sb = smem ? sizeof(float) * A.p.ntypes * smem_matrix_stride<D>(A.p.ntypes) : 0;
         if (smem)
             k_force_general<D, DBG, true><<<grid, kThreads, sb, st>>>(A);
         else
