@@ -167,54 +167,11 @@ struct TileSmem {
     int colrow[kCols];                     // grid row (y, or y + z nx) of staged column ci
     int rowid[TileCfg<D, V>::kTargets];
     int colid[TileCfg<D, V>::kTargets];
-    int seg[TileCfg<D, V>::kTargets + 1];  // first target of each segment
     int segc[TileCfg<D, V>::kTargets + 1]; // first window column of each segment
     int wsum[TileCfg<D, V>::kTargets / 32];
     int wcol[TileCfg<D, V>::kTargets / 32];
-    int nseg;
-    int staged;                         // 1: the staged columns' candidates are in smem
     float mat[kSmemMatrixMax * smem_matrix_stride<D>(kSmemMatrixMax)];
 };
-
-// Block-wide exclusive scan of v[0..n) in place (n <= kCells); returns the total.
-template <int D, int V>
-__device__ __forceinline__ int block_scan_inplace(int* v, int n, int* wsum) {
-    constexpr int kT = TileCfg<D, V>::kTargets;
-    constexpr int per = (TileCfg<D, V>::kCells + kT - 1) / kT;
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    int loc[per];
-    int sum = 0;
-#pragma unroll
-    for (int i = 0; i < per; ++i) {
-        const int e = tid * per + i;
-        loc[i] = e < n ? v[e] : 0;
-        sum += loc[i];
-    }
-    int inc = sum;
-#pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-        const int t = __shfl_up_sync(kFull, inc, d);
-        if (lane >= d) inc += t;
-    }
-    if (lane == 31) wsum[warp] = inc;
-    __syncthreads();
-    int before = 0, total = 0;
-#pragma unroll
-    for (int w = 0; w < kT / 32; ++w) {
-        const int x = wsum[w];
-        before += w < warp ? x : 0;
-        total += x;
-    }
-    int run = before + inc - sum;
-#pragma unroll
-    for (int i = 0; i < per; ++i) {
-        const int e = tid * per + i;
-        if (e < n) v[e] = run;
-        run += loc[i];
-    }
-    __syncthreads();
-    return total;
-}
 
 // Stages the cells of staged columns 0..ncols-1 (sm.colv, sm.colrow),
 // column-major: for each column the cells of its R stencil rows in turn, so
@@ -437,7 +394,6 @@ __global__ void __launch_bounds__(TileCfg<D, V>::kTargets, TileCfg<D, V>::kMinBl
     if (whole) fill_columns(0, ncol);
     if (start) {
         const int g = sbefore + __popc(bal & ((1u << lane) - 1u));
-        sm.seg[g] = tid;
         sm.segc[g] = kwin;
     }
     if (tid == 0) sm.segc[stotal] = ncol;
