@@ -446,15 +446,20 @@ __device__ __forceinline__ int staged_global(const int* coff, const int* cglob, 
 // same position) make the function return true: the caller then defers the
 // target to the FP64 fixup, which discards this partial sum.  SHIFT: some
 // candidates carry target-shift flags.
-template <int D, bool DBG, bool SHIFT>
+// SELF: the range holds the target itself at self_j; its copy is moved 8
+// units away (an exact zero term, no band or tiny flag), which sums to the
+// same bits as leaving it out, without a branch.
+template <int D, bool DBG, bool SHIFT, bool SELF = false>
 __device__ __forceinline__ bool cand_range(const ForceArgs<D>& A, const ForceParams& P, const float4* cand,
                                            const int* coff, const int* cglob, const float* __restrict__ Mrow,
-                                           int ncell, int ja, int jb, float px, float py, float pz, Acc& acc) {
+                                           int ncell, int ja, int jb, float px, float py, float pz, Acc& acc,
+                                           int self_j = -1) {
     const float px1 = px - 1.f, py1 = py - 1.f, pz1 = pz - 1.f;
     float bmin = INFINITY, dmin = INFINITY;
     const LoopK K(P);
     for (int j = ja; j < jb; ++j) {
-        const float4 q = cand[j];
+        float4 q = cand[j];
+        if (SELF && j == self_j) q.x += 8.f;
         int tb = __float_as_int(D == 3 ? q.w : q.z);
         float pxe = px, pye = py, pze = pz;
         if (SHIFT) {
@@ -464,7 +469,7 @@ __device__ __forceinline__ bool cand_range(const ForceArgs<D>& A, const ForcePar
             tb &= 0xffff;
         }
         const float d2 = eval_candidate<D>(K, q.x, q.y, q.z, pxe, pye, pze, Mrow[tb], acc, bmin, dmin);
-        if (DBG) {
+        if (DBG && !(SELF && j == self_j)) {
             acc.cand++;
             if ((d2 <= K.lo) & (d2 >= K.tiny))
                 add_pair<D, true>(acc, make_float4(0.f, 0.f, 0.f, 0.f),

@@ -414,12 +414,32 @@ __global__ void __launch_bounds__(TileCfg<D, V>::kTargets, TileCfg<D, V>::kMinBl
         const bool shift = P.wrap && (cx == nx - 1 || cy == nx - 1 || (D == 3 && cz == nx - 1));
         const int* co = sm.coff;
         const int* cg = sm.cglob;
-        if (shift) {
-            defer = cand_range<D, DBG, true>(A, P, sm.cand, co, cg, Mrow, ncell, j0, self_j, px, py, pz, acc);
-            defer |= cand_range<D, DBG, true>(A, P, sm.cand, co, cg, Mrow, ncell, self_j + 1, j1, px, py, pz, acc);
+        // 2D: three runs, before the target's own cell, the own cell (the
+        // target itself neutralised in place), after it: every lane of a cell
+        // walks the same addresses, so the candidate loads are broadcasts
+        // (2.7% faster than splitting at the target).  3D: two runs split at
+        // the target (the three-run form measured 8% slower).  Same bits.
+        const int o0 = co[own], o1 = co[own + 1];
+        if (D == 3) {
+            if (shift) {
+                defer = cand_range<D, DBG, true>(A, P, sm.cand, co, cg, Mrow, ncell, j0, self_j, px, py, pz, acc);
+                defer |= cand_range<D, DBG, true>(A, P, sm.cand, co, cg, Mrow, ncell, self_j + 1, j1, px, py, pz,
+                                                  acc);
+            } else {
+                defer = cand_range<D, DBG, false>(A, P, sm.cand, co, cg, Mrow, ncell, j0, self_j, px, py, pz, acc);
+                defer |= cand_range<D, DBG, false>(A, P, sm.cand, co, cg, Mrow, ncell, self_j + 1, j1, px, py, pz,
+                                                   acc);
+            }
+        } else if (shift) {
+            defer = cand_range<D, DBG, true>(A, P, sm.cand, co, cg, Mrow, ncell, j0, o0, px, py, pz, acc);
+            defer |= cand_range<D, DBG, true, true>(A, P, sm.cand, co, cg, Mrow, ncell, o0, o1, px, py, pz, acc,
+                                                    self_j);
+            defer |= cand_range<D, DBG, true>(A, P, sm.cand, co, cg, Mrow, ncell, o1, j1, px, py, pz, acc);
         } else {
-            defer = cand_range<D, DBG, false>(A, P, sm.cand, co, cg, Mrow, ncell, j0, self_j, px, py, pz, acc);
-            defer |= cand_range<D, DBG, false>(A, P, sm.cand, co, cg, Mrow, ncell, self_j + 1, j1, px, py, pz, acc);
+            defer = cand_range<D, DBG, false>(A, P, sm.cand, co, cg, Mrow, ncell, j0, o0, px, py, pz, acc);
+            defer |= cand_range<D, DBG, false, true>(A, P, sm.cand, co, cg, Mrow, ncell, o0, o1, px, py, pz, acc,
+                                                     self_j);
+            defer |= cand_range<D, DBG, false>(A, P, sm.cand, co, cg, Mrow, ncell, o1, j1, px, py, pz, acc);
         }
     };
     __syncthreads();
