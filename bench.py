@@ -59,7 +59,53 @@ BYTES = {"scatter": WORK["PLG_WORK_SCATTER_BYTES"], "gather": WORK["PLG_WORK_GAT
          "force": WORK["PLG_WORK_FORCE_BYTES_2D"], "scan_cell": WORK["PLG_WORK_SCAN_BYTES_PER_CELL"]}
 
 
-def parse():
+class Replicas:
+    """The replicas path of a multi-GPU run: one process per GPU, each
+    stepping its own world; no collective on the data path.  Reads
+    RANK / WORLD_SIZE / LOCAL_RANK from the environment (torchrun); with more
+    than one rank it joins a process group (`backend`: nccl on GPUs, gloo for
+    the CPU tests).  The timed region's duration is the maximum over ranks and
+    a whole-job rate is all ranks' units over that time; only rank 0 prints."""
+
+    def __init__(self, backend: str = "nccl"):
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.world_size = int(os.environ.get("WORLD_SIZE", "1"))
+        self.local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+        self.dist = None
+        if self.world_size > 1:
+            import torch.distributed as dist
+
+            dist.init_process_group(backend)
+            self.dist = dist
+
+    @property
+    def leader(self) -> bool:
+        return self.rank == 0
+
+    def barrier(self) -> None:
+        if self.dist is not None:
+            self.dist.barrier()
+
+    def max_over_ranks(self, x: float, device=None) -> float:
+        if self.dist is None:
+            return float(x)
+        import torch
+
+        t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def rate(self, units_per_rank: float, seconds: float, device=None) -> float:
+        """Whole-job rate: units of all ranks / the slowest rank's time."""
+        return self.world_size * units_per_rank / self.max_over_ranks(seconds, device)
+
+    def close(self) -> None:
+        if self.dist is not None:
+            self.dist.destroy_process_group()
+            self.dist = None
+
+
+def parse(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=200)
@@ -78,7 +124,7 @@ def parse():
     ap.add_argument("--steps-3d", type=int, default=20)
     ap.add_argument("--serve-seconds", type=float, default=10.0)
     ap.add_argument("--serve-rate", type=float, default=200.0)
-    return ap.parse_args()
+    return ap.parse_args(argv)
 
 
 def make_world(n: int, seed: int = 2024):
@@ -309,8 +355,8 @@ def run_serving(args) -> dict:
 
 
 def run_reference(args):
-    rank = int(os.environ.get("RANK", "0"))
-    if rank != 0:
+    # The reference is a CPU path: rank 0 alone times it, the other ranks exit.
+    if int(os.environ.get("RANK", "0")) != 0:
         return
     threads = os.cpu_count() or 1
     import orc
@@ -345,17 +391,9 @@ def run_ours(args):
     from plgpu import _lib
     from plgpu.physics import GpuWorld
 
-    rank = int(os.environ.get("RANK", "0"))
-    world_size = int(os.environ.get("WORLD_SIZE", "1"))
-    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
-    dist = None
-    if world_size > 1:
-        import torch.distributed as dist
-
-        torch.cuda.set_device(local_rank)
-        dist.init_process_group("nccl")
-    else:
-        torch.cuda.set_device(0)
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    reps = Replicas("nccl")
+    rank, world_size = reps.rank, reps.world_size
     dev = torch.device("cuda", torch.cuda.current_device())
 
     import __graft_entry__
@@ -378,8 +416,7 @@ def run_ours(args):
         torch.cuda.synchronize()
 
     def barrier():
-        if dist is not None:
-            dist.barrier()
+        reps.barrier()
         torch.cuda.synchronize()
 
     check = plgpu.physics.check
@@ -397,13 +434,9 @@ def run_ours(args):
         ev[k][1].record(stream)
         check(lib.plg_sync(w.ctx, 60.0), w.ctx, "plg_sync")
     barrier()
-    total_ms = sum(a.elapsed_time(b) for a, b in ev)
-    if dist is not None:
-        t = torch.tensor([total_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = reps.max_over_ranks(sum(a.elapsed_time(b) for a, b in ev), dev)
     ms_per_step = total_ms / args.steps
-    value = world_size * n * args.steps / (total_ms * 1e-3)
+    value = reps.rate(n * args.steps, total_ms * 1e-3, dev)
 
     # per-kernel durations over a profiled pass of the same number of steps
     check(lib.plg_profile_enable(w.ctx, 1), w.ctx, "plg_profile_enable")
@@ -442,11 +475,8 @@ def run_ours(args):
         parts += (t1 - t0, t2 - t1, t3 - t2)
     barrier()
     clk = clocks.stop()
-    if dist is not None:
-        t = torch.tensor([e2e_s], device=dev, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e_value = world_size * n * args.e2e_steps / e2e_s
+    e2e_s = reps.max_over_ranks(e2e_s, dev)
+    e2e_value = reps.rate(n * args.e2e_steps, e2e_s, dev)
 
     deferred = w.deferred()
     # pair statistics of the current state (one instrumented step)
@@ -532,8 +562,7 @@ def run_ours(args):
             "clocks": clk,
         }
         print(json.dumps(line))
-    if dist is not None:
-        dist.destroy_process_group()
+    reps.close()
 
 
 def main():
