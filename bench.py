@@ -496,17 +496,23 @@ def run_ours(args):
     force_us = kern["force"]["avg_us"]
     flops = n * (cand * FLOPS_PER_CANDIDATE[2] + inter * FLOPS_PER_INTERACTION[2])
     achieved = flops / (force_us * 1e-6) / 1e12
-    traffic = None
+    traffic = issue_active = None
     tf = REPO / "profiles" / "k_force_tile_2d_1m.md"  # ncu summary of this kernel on this workload
     if tf.exists():
-
-        mt = re.search(r"^dram_bytes_per_launch: (\d+)", tf.read_text(), re.M)
+        text = tf.read_text()
+        mt = re.search(r"^dram_bytes_per_launch: (\d+)", text, re.M)
         traffic = int(mt.group(1)) if mt else None
+        mi = re.search(r"^\| smsp__issue_active \(% of active cycles\) \| ([\d.]+)%", text, re.M)
+        issue_active = float(mi.group(1)) / 100 if mi else None
     roofline = {"bound": "fp32", "kernel": "force", "achieved": achieved, "peak": peak.value, "unit": "TFLOP/s",
                 "frac": achieved / peak.value, "traffic": traffic,
                 "peak_source": "FFMA microbenchmark run live by this bench (MEASURED_PEAKS.json has no FP32 peak)",
                 "work": f"{cand:.2f} candidate + {inter:.2f} interacting pairs per particle; "
-                        f"{FLOPS_PER_CANDIDATE[2]} / {FLOPS_PER_INTERACTION[2]} flops each"}
+                        f"{FLOPS_PER_CANDIDATE[2]} / {FLOPS_PER_INTERACTION[2]} flops each",
+                # What actually bounds the kernel: instruction issue (compares,
+                # selects, shared-memory loads and the rsqrt beside the FMAs),
+                # as ncu measured it on this workload.
+                "issue_active_ncu": issue_active}
     sort_kernels = {}
     if hbm:
         cells = (int(np.floor(1 / SETTINGS["rmax"]))) ** 2
