@@ -132,8 +132,11 @@ __global__ void __launch_bounds__(kThreads) k_force_general(const __grid_constan
 //               blocks with spilled registers measured slower)
 //   kCap        staged candidates per segment
 //   kCells      stencil cells per segment (R x columns)
-// Variant 0 suits dense worlds; variant 1 (smaller tiles, less shared memory,
-// more resident blocks) suits sparse ones, where a tile spans many rows.
+// 2D: variant 0 suits the 1M-particle world (a few cells per tile); variant
+// 1 (half the targets, a staging for 2560 candidates) suits very dense worlds
+// (hundreds of particles per cell), where variant 0's windows overflow; it
+// won the autotuner on the batched benchmark (6.24 vs 6.33 ms per step).
+// 3D: variant 1 is the smaller tile for sparse worlds.
 template <int D, int V>
 struct TileCfg;
 template <>
@@ -142,7 +145,7 @@ struct TileCfg<2, 0> {
 };
 template <>
 struct TileCfg<2, 1> {
-    static constexpr int kTargets = 128, kMinBlocks = 8, kCap = 1024, kCells = 512;
+    static constexpr int kTargets = 128, kMinBlocks = 6, kCap = 2560, kCells = 768;
 };
 template <>
 struct TileCfg<3, 0> {

@@ -172,15 +172,15 @@ def test_empty_and_single(gpu):
 
 @pytest.mark.parametrize("dim", [2, 3])
 def test_staged_and_global_memory_paths_agree(gpu, dim):
-    """A world whose segments overflow shared memory under one tile variant
+    """A world whose windows overflow shared memory under one tile variant
     and fit under the other: the staged and the global-memory paths walk the
     same candidates in the same order, so the two runs agree bit for bit."""
     from plgpu.batch import GpuBatch, WorldDesc
 
-    # ~115 per cell (2D) and ~20 per cell (3D): a 128-target tile overflows
-    # variant 1's staging (1024 / 1280 candidates), a tile of variant 0
-    # (1536 / 2560) mostly fits.
-    spec = (uniform_world(46_000, 5, 0.05, seed=17, vel_scale=0.01) if dim == 2 else
+    # 2D: ~220 per cell, a 9-cell window of ~1980 candidates overflows variant
+    # 0's staging (1536) and fits variant 1's (2560).  3D: ~20 per cell, a
+    # 128-target tile of variant 0 stages whole, variant 1 (1024) in chunks.
+    spec = (uniform_world(88_000, 5, 0.05, seed=17, vel_scale=0.01) if dim == 2 else
             uniform_world(20_000, 6, 0.1, seed=18, dim=3, vel_scale=0.01))
     runs = []
     for variant in (0, 1):
