@@ -11,7 +11,9 @@ Our arm (default):
   value  device-resident state; each step timed alone with CUDA events on the
          library's stream; L2 flushed (256 MB write) between steps.
   e2e    the public API with host buffers: per step plg_upload (pinned host
-         double/int arrays) + plg_step + plg_download, host wall clock.
+         double/int arrays) + plg_step_download (one step whose force kernel
+         writes the snapshot to the host arrays), host wall clock; "unfused"
+         beside it: plg_upload + plg_step + plg_download.
   roofline of the dominant kernel (the force kernel), from per-kernel CUDA
          events over a profiled pass of the same steps.
   cpu_baseline  the oracle (C FP64 restatement of the reference's step, all
@@ -473,10 +475,29 @@ def run_ours(args):
         t3 = time.perf_counter()
         e2e_s += t3 - t0
         parts += (t1 - t0, t2 - t1, t3 - t2)
+    # the same with the download fused into the step (plg_step_download)
+    fused_s = 0.0
+    fparts = np.zeros(2)
+    fuses = _lib.C.c_int32(0)
+    check(lib.plg_step_download_fuses(w.ctx, _lib.ptr(hp, P), _lib.ptr(hv, P), _lib.ptr(ht, I), _lib.ptr(hi, I),
+                                      _lib.C.byref(fuses)), w.ctx, "plg_step_download_fuses")
+    barrier()
+    for k in range(args.e2e_steps):
+        flush_l2()
+        t0 = time.perf_counter()
+        check(lib.plg_upload(w.ctx, n, _lib.ptr(hp, P), _lib.ptr(hv, P), _lib.ptr(ht, I)), w.ctx, "plg_upload")
+        t1 = time.perf_counter()
+        check(lib.plg_step_download(w.ctx, 1, _lib.ptr(hp, P), _lib.ptr(hv, P), _lib.ptr(ht, I), _lib.ptr(hi, I)),
+              w.ctx, "plg_step_download")
+        t2 = time.perf_counter()
+        fused_s += t2 - t0
+        fparts += (t1 - t0, t2 - t1)
     barrier()
     clk = clocks.stop()
     e2e_s = reps.max_over_ranks(e2e_s, dev)
-    e2e_value = reps.rate(n * args.e2e_steps, e2e_s, dev)
+    unfused_value = reps.rate(n * args.e2e_steps, e2e_s, dev)
+    fused_s = reps.max_over_ranks(fused_s, dev)
+    e2e_value = reps.rate(n * args.e2e_steps, fused_s, dev)
 
     deferred = w.deferred()
     # pair statistics of the current state (one instrumented step)
@@ -551,8 +572,12 @@ def run_ours(args):
                        "l2": "warm (not flushed)" if args.no_flush else "flushed (256 MB write) between steps"},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": n * (24 + 24 + 4),
                     "d2h_bytes_per_step": n * (24 + 24 + 4 + 4), "steps": args.e2e_steps,
-                    "api": "plg_upload + plg_step + plg_download, pinned host buffers, host wall clock",
-                    "ms_upload_step_download": [round(1e3 * x / args.e2e_steps, 4) for x in parts]},
+                    "api": "plg_upload + plg_step_download (the force kernel writes the snapshot), pinned host "
+                           "buffers, host wall clock",
+                    "snapshot_fused": bool(fuses.value),
+                    "ms_upload_stepdownload": [round(1e3 * x / args.e2e_steps, 4) for x in fparts],
+                    "unfused": {"value": unfused_value, "api": "plg_upload + plg_step + plg_download",
+                                "ms_upload_step_download": [round(1e3 * x / args.e2e_steps, 4) for x in parts]}},
             "deferred_targets_last_step": deferred,
             "gpu_launches": len(_lib.KERNELS) * args.steps,
             "roofline": roofline,

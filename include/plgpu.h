@@ -139,6 +139,26 @@ int plg_sync(plg_ctx* ctx, double timeout_s);
 int plg_download(plg_ctx* ctx, double* pos, double* vel, int32_t* type,
                  int32_t* id);
 
+/* plg_step(ctx, nsteps) then plg_download(ctx, pos, vel, type, id), with the
+ * same results, errors and stop behaviour (a stopped call writes nothing).
+ * This is the app's update-then-snapshot pair: updatePhysics
+ * (app/Main.java:292-295) followed by physicsSnapshot.take
+ * (app/Main.java:600-603, app/PhysicsSnapshot.java:24-62).  When every
+ * non-NULL array is device-accessible, the last step's force kernel writes
+ * the snapshot as it finishes each particle, so the host-link transfer
+ * overlaps the step.
+ * Device-accessible means page-locked, or pageable memory on a device with
+ * coherent pageable access.  Otherwise the call is plg_step followed by
+ * plg_download. */
+int plg_step_download(plg_ctx* ctx, int32_t nsteps, double* pos, double* vel,
+                      int32_t* type, int32_t* id);
+
+/* *fused = 1 when plg_step_download with these arrays (and the current
+ * settings and particle count) writes them from the force kernel, else 0. */
+int plg_step_download_fuses(plg_ctx* ctx, const double* pos, const double* vel,
+                            const int32_t* type, const int32_t* id,
+                            int32_t* fused);
+
 int plg_particle_count(plg_ctx* ctx, int64_t* n);
 
 /* ---- initialisers on the device ------------------------------------------ */

@@ -26,6 +26,7 @@ struct ForceArgs {
     uint32_t* counts;
     uint32_t* defer_count;  // targets the tiled kernel deferred this step (statistics)
     DebugOut dbg;
+    HostSnap snap;  // snapshot arrays written by the tiled kernel's SNAP form
     // Batched worlds: per-world parameters, first sorted slots
     // (wp_off[k] = worlds[k].p_off) and first tiles (tile_off[k] = the sum
     // of ceil(n_j / kTargets) over j < k), nworlds + 1 entries each.
@@ -585,6 +586,47 @@ __device__ __noinline__ void fixup_target(const ForceArgs<D>& A, const ForcePara
     }
 }
 
+// The snapshot of one warp's slots w0 .. w0+m-1 (m <= 32; the whole warp
+// calls): the values this warp's epilogue and fixups stored in A, read back
+// and written in the plg_download layout.  pos and vel are 3 doubles per
+// particle, so the warp's 32 particles are 96 consecutive doubles of each;
+// lane l writes doubles l, l+32 and l+64 (particle j/3, component j%3,
+// fetched from its lane by shuffles), so every store instruction covers
+// 256 contiguous bytes.
+template <int D>
+__device__ __forceinline__ void write_snapshot_warp(const ForceArgs<D>& A, int w0, int m, int lane) {
+    if (m <= 0) return;  // warp-uniform
+    __syncwarp();        // the lanes' stores to A (epilogue, fixups) are visible to the warp
+    float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
+    typename Layout<D>::Vel v{};
+    const bool mine = lane < m;
+    if (mine) {
+        p = A.apt[w0 + lane];
+        v = A.avel[w0 + lane];
+    }
+    const float c0 = p.x, c1 = p.y, c2 = D == 3 ? p.z : 0.f;
+    float u2 = 0.f;
+    if constexpr (D == 3) u2 = v.z;
+    const float u0 = v.x, u1 = v.y;
+    double* pos = A.snap.pos ? A.snap.pos + 3 * (size_t)w0 : nullptr;
+    double* vel = A.snap.vel ? A.snap.vel + 3 * (size_t)w0 : nullptr;
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+        const int j = 32 * r + lane;
+        const int q = j / 3, k = j - 3 * q;
+        const float a0 = __shfl_sync(kFull, c0, q), a1 = __shfl_sync(kFull, c1, q), a2 = __shfl_sync(kFull, c2, q);
+        const float b0 = __shfl_sync(kFull, u0, q), b1 = __shfl_sync(kFull, u1, q), b2 = __shfl_sync(kFull, u2, q);
+        if (q < m) {
+            if (pos) pos[j] = (double)(k == 0 ? a0 : (k == 1 ? a1 : a2));
+            if (vel) vel[j] = (double)(k == 0 ? b0 : (k == 1 ? b1 : b2));
+        }
+    }
+    if (mine) {
+        if (A.snap.type) A.snap.type[w0 + lane] = Layout<D>::type(p);
+        if (A.snap.id) A.snap.id[w0 + lane] = Layout<D>::id(p, v);
+    }
+}
+
 template <int D>
 ForceArgs<D> make_args(const ForceParams& p, StateBuf<D> b, const uint32_t* cstart, const uint32_t* slot_cell,
                        StateBuf<D> a, uint32_t* cell, uint32_t* counts, uint32_t* defer, const DebugOut* dbg) {
@@ -600,6 +642,7 @@ ForceArgs<D> make_args(const ForceParams& p, StateBuf<D> b, const uint32_t* csta
     A.counts = counts;
     A.defer_count = defer;
     A.dbg = dbg ? *dbg : DebugOut{nullptr, nullptr, nullptr, nullptr, nullptr};
+    A.snap = HostSnap{nullptr, nullptr, nullptr, nullptr};
     A.worlds = nullptr;
     A.wp_off = nullptr;
     A.tile_off = nullptr;

@@ -292,9 +292,13 @@ __device__ __forceinline__ bool stage_columns(const ForceArgs<D>& A, const Force
 // so a block never mixes worlds and every world is cut into exactly the
 // tiles a single-world launch uses: each world computes bit for bit what
 // plg_step computes for it, whatever else is in the batch.
-template <int D, bool DBG, bool SMEM_M, bool BATCH, int V>
+//
+// SNAP (single world, not instrumented): each warp also writes its slots'
+// new state to the snapshot arrays A.snap once its deferred targets are done.
+template <int D, bool DBG, bool SMEM_M, bool BATCH, int V, bool SNAP = false>
 __global__ void __launch_bounds__(TileCfg<D, V>::kTargets, TileCfg<D, V>::kMinBlocks)
     k_force_tile(const __grid_constant__ ForceArgs<D> A) {
+    static_assert(!SNAP || (!DBG && !BATCH), "the snapshot form is the plain single-world kernel");
     constexpr int kT = TileCfg<D, V>::kTargets;
     constexpr int R = TileRows<D>::R;
     extern __shared__ __align__(16) unsigned char smraw[];
@@ -499,6 +503,7 @@ __global__ void __launch_bounds__(TileCfg<D, V>::kTargets, TileCfg<D, V>::kMinBl
         dm &= dm - 1;
         fixup_target<D, DBG>(A, P, cs, M, __shfl_sync(kFull, s, src), lane);
     }
+    if constexpr (SNAP) write_snapshot_warp<D>(A, s0 + 32 * warp, min(32, nvalid - 32 * warp), lane);
 }
 
 template <int D, bool DBG, bool BATCH, int V>
@@ -507,6 +512,15 @@ void launch_tile(cudaStream_t st, const ForceArgs<D>& A, bool smem_matrix, int b
     const int grid = BATCH ? batch_tiles : (A.n_total + kT - 1) / kT;
     if (grid <= 0) return;
     const size_t sb = sizeof(TileSmem<D, V>);
+    if constexpr (!DBG && !BATCH) {
+        if (A.snap.any()) {
+            if (smem_matrix)
+                k_force_tile<D, false, true, false, V, true><<<grid, kT, sb, st>>>(A);
+            else
+                k_force_tile<D, false, false, false, V, true><<<grid, kT, sb, st>>>(A);
+            return;
+        }
+    }
     if (smem_matrix)
         k_force_tile<D, DBG, true, BATCH, V><<<grid, kT, sb, st>>>(A);
     else
@@ -542,9 +556,10 @@ void launch_variant(cudaStream_t st, const ForceArgs<D>& A, bool general, int va
 template <int D>
 void launch_force(cudaStream_t st, const ForceParams& p, bool general, StateBuf<D> b, const uint32_t* cstart,
                   const uint32_t* slot_cell, StateBuf<D> a, uint32_t* cell, uint32_t* counts, uint32_t* defer,
-                  const DebugOut* dbg, int variant) {
+                  const DebugOut* dbg, int variant, const HostSnap* snap) {
     if (p.n <= 0) return;
-    const ForceArgs<D> A = make_args<D>(p, b, cstart, slot_cell, a, cell, counts, defer, dbg);
+    ForceArgs<D> A = make_args<D>(p, b, cstart, slot_cell, a, cell, counts, defer, dbg);
+    if (snap && !dbg && !general) A.snap = *snap;
     if (dbg)
         launch_variant<D, true>(st, A, general, variant);
     else
@@ -584,14 +599,16 @@ template void launch_force_batch<3>(cudaStream_t, const ForceParams*, const int*
                                     uint32_t*, uint32_t*, const DebugOut*, int);
 
 template void launch_force<2>(cudaStream_t, const ForceParams&, bool, StateBuf<2>, const uint32_t*, const uint32_t*,
-                              StateBuf<2>, uint32_t*, uint32_t*, uint32_t*, const DebugOut*, int);
+                              StateBuf<2>, uint32_t*, uint32_t*, uint32_t*, const DebugOut*, int,
+                              const HostSnap*);
 template void launch_force<3>(cudaStream_t, const ForceParams&, bool, StateBuf<3>, const uint32_t*, const uint32_t*,
-                              StateBuf<3>, uint32_t*, uint32_t*, uint32_t*, const DebugOut*, int);
+                              StateBuf<3>, uint32_t*, uint32_t*, uint32_t*, const DebugOut*, int,
+                              const HostSnap*);
 
-template <int D, bool DBG, bool SMEM_M, bool BATCH, int V>
+template <int D, bool DBG, bool SMEM_M, bool BATCH, int V, bool SNAP = false>
 cudaError_t allow_one() {
-    return cudaFuncSetAttribute(k_force_tile<D, DBG, SMEM_M, BATCH, V>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)sizeof(TileSmem<D, V>));
+    return cudaFuncSetAttribute(k_force_tile<D, DBG, SMEM_M, BATCH, V, SNAP>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(TileSmem<D, V>));
 }
 
 template <int D, int V>
@@ -599,7 +616,8 @@ cudaError_t allow_tile_smem() {
     const cudaError_t es[] = {allow_one<D, false, true, false, V>(), allow_one<D, false, false, false, V>(),
                               allow_one<D, true, true, false, V>(),  allow_one<D, true, false, false, V>(),
                               allow_one<D, false, true, true, V>(),  allow_one<D, false, false, true, V>(),
-                              allow_one<D, true, true, true, V>(),   allow_one<D, true, false, true, V>()};
+                              allow_one<D, true, true, true, V>(),   allow_one<D, true, false, true, V>(),
+                              allow_one<D, false, true, false, V, true>(), allow_one<D, false, false, false, V, true>()};
     for (cudaError_t e : es)
         if (e != cudaSuccess) return e;
     return cudaSuccess;

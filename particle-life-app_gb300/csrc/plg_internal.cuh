@@ -167,6 +167,19 @@ struct DebugOut {
     unsigned long long* candidates;
 };
 
+// Snapshot arrays the force kernel writes besides the next state, in the
+// plg_download layout (pos and vel: 3 doubles per particle, z = 0 in 2D;
+// type and id: one int32 each), indexed by sorted slot.  Each pointer is
+// device-accessible (page-locked host memory's device alias, or pageable
+// memory on a device with coherent pageable access) or null (not written).
+struct HostSnap {
+    double* pos;
+    double* vel;
+    int32_t* type;
+    int32_t* id;
+    __host__ __device__ bool any() const { return pos || vel || type || id; }
+};
+
 template <int D>
 struct StateBuf {
     float4* pt;
@@ -285,10 +298,12 @@ void launch_gather(cudaStream_t st, int n, const uint32_t* perm, const uint32_t*
 // `defer`: one word, zeroed before the step; counts the targets the tiled
 // kernel recomputed in its deferred pass.
 // variant: tile variant of the force kernel (0 or 1, the autotuner's knob).
+// snap (tiled kernel only, not with dbg; may be null): also write the new
+// state to these arrays (see HostSnap).
 template <int D>
 void launch_force(cudaStream_t st, const ForceParams& p, bool general, StateBuf<D> b, const uint32_t* cstart,
                   const uint32_t* slot_cell, StateBuf<D> a, uint32_t* cell, uint32_t* counts, uint32_t* defer,
-                  const DebugOut* dbg, int variant = 0);
+                  const DebugOut* dbg, int variant = 0, const HostSnap* snap = nullptr);
 
 // Batched worlds: `worlds` (device, nworlds entries) holds each world's
 // parameters with its cell_base and p_off; `wp_off` (device, nworlds + 1)

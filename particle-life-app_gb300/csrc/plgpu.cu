@@ -104,6 +104,29 @@ T* host_mapped(T* p) {
     return static_cast<T*>(a.devicePointer);
 }
 
+// The address a kernel writes host array p through: the device alias of
+// page-locked memory, or p itself when it is pageable and the device
+// accesses pageable memory coherently.  False: neither (p != NULL).
+template <typename T>
+bool kernel_writable(T* p, bool pageable, T** out) {
+    *out = nullptr;
+    if (!p) return true;
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    if (a.type == cudaMemoryTypeHost && a.devicePointer) {
+        *out = static_cast<T*>(a.devicePointer);
+        return true;
+    }
+    if (a.type == cudaMemoryTypeUnregistered && pageable) {
+        *out = p;
+        return true;
+    }
+    return false;
+}
+
 }  // namespace
 
 struct plg_ctx {
@@ -112,6 +135,7 @@ struct plg_ctx {
     int64_t n = 0;
     int64_t next_id = 0;  // id of the next particle added (plg_append)
     int device = 0;
+    bool pageable = false;  // the device accesses pageable host memory coherently
     cudaStream_t stream = nullptr;
 
     plg_settings s{};
@@ -264,8 +288,9 @@ void compute_force_params(plg_ctx* c) {
 Grid grid_of(plg_ctx* c) { return c->fp.g; }
 
 // Enqueues the body of one step (no rebin) on c->stream.
+// snap (may be null): snapshot arrays the force kernel also writes.
 template <int D>
-void enqueue_body(plg_ctx* c, const DebugOut* dbg, int32_t* cell_sorted) {
+void enqueue_body(plg_ctx* c, const DebugOut* dbg, int32_t* cell_sorted, const HostSnap* snap = nullptr) {
     cudaStream_t st = c->stream;
     const int n = (int)c->n;
     auto k0 = [&](int k) {
@@ -286,15 +311,23 @@ void enqueue_body(plg_ctx* c, const DebugOut* dbg, int32_t* cell_sorted) {
     k1(PLG_K_GATHER);
     k0(PLG_K_FORCE);
     launch_force<D>(st, c->fp, c->general, buf_b<D>(c), c->cstart, c->slot_cell, buf_a<D>(c), c->cell, c->counts,
-                    c->defer, dbg);
+                    c->defer, dbg, 0, snap);
     k1(PLG_K_FORCE);
 }
 
-void enqueue_body_dim(plg_ctx* c, const DebugOut* dbg, int32_t* cell_sorted) {
+void enqueue_body_dim(plg_ctx* c, const DebugOut* dbg, int32_t* cell_sorted, const HostSnap* snap = nullptr) {
     if (c->dim == 2)
-        enqueue_body<2>(c, dbg, cell_sorted);
+        enqueue_body<2>(c, dbg, cell_sorted, snap);
     else
-        enqueue_body<3>(c, dbg, cell_sorted);
+        enqueue_body<3>(c, dbg, cell_sorted, snap);
+}
+
+// True when the force kernel can write the snapshot arrays itself (the
+// tiled kernel runs and every non-null array is kernel-writable); fills hs.
+bool snapshot_fusable(plg_ctx* c, double* pos, double* vel, int32_t* type, int32_t* id, HostSnap* hs) {
+    return !c->general && c->n > 0 && kernel_writable(pos, c->pageable, &hs->pos) &&
+           kernel_writable(vel, c->pageable, &hs->vel) && kernel_writable(type, c->pageable, &hs->type) &&
+           kernel_writable(id, c->pageable, &hs->id);
 }
 
 int enqueue_rebin(plg_ctx* c) {
@@ -471,11 +504,14 @@ int plg_create(int dim, int64_t capacity, plg_ctx** out) {
     c->dim = dim;
     c->cap = capacity;
     cudaError_t e = cudaGetDevice(&c->device);
+    int pageable = 0;
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, c->device);
     if (e != cudaSuccess) {
         cudaGetLastError();
         delete c;
         return PLG_E_CUDA;
     }
+    c->pageable = pageable != 0;
     int rc = PLG_OK;
     const size_t vel_sz = dim == 2 ? sizeof(float2) : sizeof(float4);
     auto dmalloc = [&](void** p, size_t bytes) {
@@ -719,6 +755,54 @@ int plg_download(plg_ctx* c, double* pos, double* vel, int32_t* type, int32_t* i
     }
     CK(c, cudaStreamSynchronize(st));
     return PLG_OK;
+}
+
+int plg_step_download_fuses(plg_ctx* c, const double* pos, const double* vel, const int32_t* type,
+                            const int32_t* id, int32_t* fused) {
+    if (!c || !fused) return PLG_E_INVALID_ARG;
+    int rc = check_ready(c);
+    if (rc) return rc;
+    DeviceGuard g(c->device);
+    HostSnap hs{nullptr, nullptr, nullptr, nullptr};
+    *fused = snapshot_fusable(c, const_cast<double*>(pos), const_cast<double*>(vel), const_cast<int32_t*>(type),
+                              const_cast<int32_t*>(id), &hs)
+                 ? 1
+                 : 0;
+    return PLG_OK;
+}
+
+int plg_step_download(plg_ctx* c, int32_t nsteps, double* pos, double* vel, int32_t* type, int32_t* id) {
+    int rc = check_ready(c);
+    if (rc) return rc;
+    if (nsteps < 0) return set_err(c, PLG_E_INVALID_ARG, "negative step count");
+    if (nsteps == 0) return plg_download(c, pos, vel, type, id);
+    DeviceGuard g(c->device);
+    HostSnap hs{nullptr, nullptr, nullptr, nullptr};
+    if (!snapshot_fusable(c, pos, vel, type, id, &hs)) {
+        if ((rc = plg_step(c, nsteps))) return rc;
+        return plg_download(c, pos, vel, type, id);
+    }
+    auto stopped = [&]() {
+        const std::string m = c->err;
+        const int r2 = plg_sync(c, 0);
+        if (r2) return r2;
+        c->err = m;
+        return (int)PLG_E_STOPPED;
+    };
+    rc = plg_step_async(c, nsteps - 1);
+    if (rc == PLG_E_STOPPED) return stopped();
+    if (rc) return rc;
+    if (c->stop.exchange(0)) {
+        set_err(c, PLG_E_STOPPED, "stopped by plg_request_stop");
+        return stopped();
+    }
+    // The last step, as plain launches: its force kernel carries the
+    // caller's arrays, which change from call to call.
+    if ((rc = enqueue_rebin(c))) return rc;
+    enqueue_body_dim(c, nullptr, nullptr, &hs);
+    CK(c, cudaGetLastError());
+    if (c->profiling && (rc = accumulate_profile(c))) return rc;
+    return plg_sync(c, 0);
 }
 
 }  // extern "C"

@@ -141,6 +141,8 @@ SIGNATURES = {
     "plg_step_async": (C.c_int, [_P, C.c_int32]),
     "plg_sync": (C.c_int, [_P, C.c_double]),
     "plg_download": (C.c_int, [_P, _DP, _DP, _I32P, _I32P]),
+    "plg_step_download": (C.c_int, [_P, C.c_int32, _DP, _DP, _I32P, _I32P]),
+    "plg_step_download_fuses": (C.c_int, [_P, _DP, _DP, _I32P, _I32P, C.POINTER(C.c_int32)]),
     "plg_particle_count": (C.c_int, [_P, _I64P]),
     "plg_request_stop": (C.c_int, [_P]),
     "plg_last_error": (C.c_char_p, [_P]),

@@ -289,6 +289,34 @@ class GpuWorld:
         )
         return pos, vel, types, ids
 
+    def step_download(self, nsteps: int = 1, out=None):
+        """`nsteps` steps, then the state in the download() layout
+        (plg_step_download: the last step's force kernel writes the arrays
+        when they are page-locked, or pageable on a device that accesses
+        pageable memory).  `out`: optional (pos, vel, types, ids) arrays of
+        the download() shapes and dtypes to fill (any may be None)."""
+        n = self.count()
+        if out is None:
+            out = (np.empty((n, 3), np.float64), np.empty((n, 3), np.float64),
+                   np.empty(n, np.int32), np.empty(n, np.int32))
+        pos, vel, types, ids = out
+        for a, shape, dt in ((pos, (n, 3), np.float64), (vel, (n, 3), np.float64),
+                             (types, (n,), np.int32), (ids, (n,), np.int32)):
+            if a is not None and (a.shape != shape or a.dtype != dt or not a.flags.c_contiguous):
+                raise ValueError("step_download: output arrays must be C-contiguous with the download() shapes")
+        self._c(
+            self.lib.plg_step_download(
+                self.ctx,
+                nsteps,
+                _lib.ptr(pos, _lib.C.c_double),
+                _lib.ptr(vel, _lib.C.c_double),
+                _lib.ptr(types, _lib.C.c_int32),
+                _lib.ptr(ids, _lib.C.c_int32),
+            ),
+            "plg_step_download",
+        )
+        return pos, vel, types, ids
+
     def debug_step(self):
         """One step with the instrumented kernel: per-particle cell, pair
         count, pair hashes, FP32 accelerations (cell-sorted order)."""

@@ -38,7 +38,7 @@ def spec_for(case):
     if case == "2d_many_types":
         return uniform_world(40_000, 100, 0.01, seed=7, vel_scale=0.01)
     if case == "2d_small_grid":
-        return uniform_world(3000, 4, 0.3, seed=5, vel_scale=0.01)
+        return uniform_world(3000, 4, 0.4, seed=5, vel_scale=0.01)  # nx = 2: the literal path
     if case == "3d_uniform":
         return uniform_world(100_000, 8, 0.03, seed=42, dim=3, vel_scale=0.01, dt=0.01)
     if case == "3d_blobs":
