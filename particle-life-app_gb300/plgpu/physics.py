@@ -297,8 +297,9 @@ class GpuWorld:
         the download() shapes and dtypes to fill (any may be None)."""
         n = self.count()
         if out is None:
-            out = (np.empty((n, 3), np.float64), np.empty((n, 3), np.float64),
-                   np.empty(n, np.int32), np.empty(n, np.int32))
+            # Written by the CPU first (np.full), so every page is resident
+            # before the device writes the arrays in place.
+            out = (np.full((n, 3), 0.0), np.full((n, 3), 0.0), np.full(n, 0, np.int32), np.full(n, 0, np.int32))
         pos, vel, types, ids = out
         for a, shape, dt in ((pos, (n, 3), np.float64), (vel, (n, 3), np.float64),
                              (types, (n,), np.int32), (ids, (n,), np.int32)):
