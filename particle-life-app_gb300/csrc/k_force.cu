@@ -16,9 +16,10 @@
 // the block stages the sorted union of its targets' windows into shared
 // memory column by column, each column's R cells in turn, so that every
 // target's neighbourhood is one contiguous run.  When the whole block's
-// windows fit, one staging serves every target; otherwise each segment is
-// staged in chunks of columns, halved until they fit, and a single window
-// that still does not fit (a very dense region) is read from global memory
+// windows fit, one staging serves every target; otherwise the block's
+// columns are staged in chunks (which may span segments), halved until they
+// fit, and a single window that still does not fit (a very dense region) is
+// read from global memory
 // in the same candidate order (direct_stencil), giving the same bits.  The
 // candidate loop is branch-free FP32.  A target that meets a candidate
 // needing the FP64 decision is deferred: its warp recomputes it from global
@@ -130,8 +131,8 @@ __global__ void __launch_bounds__(kThreads) k_force_general(const __grid_constan
 //   kTargets    targets per block, one thread each
 //   kMinBlocks  resident blocks per SM asked for (caps the registers: more
 //               blocks with spilled registers measured slower)
-//   kCap        staged candidates per segment
-//   kCells      stencil cells per segment (R x columns)
+//   kCap        staged candidates per staging
+//   kCells      stencil cells per staging (R x columns)
 // 2D: variant 0 suits the 1M-particle world (a few cells per tile); variant
 // 1 (half the targets, a staging for 2560 candidates) suits very dense worlds
 // (hundreds of particles per cell), where variant 0's windows overflow; it
@@ -170,7 +171,6 @@ struct TileSmem {
     int colrow[kCols];                     // grid row (y, or y + z nx) of staged column ci
     int rowid[TileCfg<D, V>::kTargets];
     int colid[TileCfg<D, V>::kTargets];
-    int segc[TileCfg<D, V>::kTargets + 1]; // first window column of each segment
     int wsum[TileCfg<D, V>::kTargets / 32];
     int wcol[TileCfg<D, V>::kTargets / 32];
     float mat[kSmemMatrixMax * smem_matrix_stride<D>(kSmemMatrixMax)];
@@ -361,25 +361,19 @@ __global__ void __launch_bounds__(TileCfg<D, V>::kTargets, TileCfg<D, V>::kMinBl
     const bool start = valid && (tid == 0 || sm.rowid[tid - 1] != row);
     const bool lead = valid && (start || pcol != cx);
     const int newc = !lead ? 0 : (start ? 3 : min(3, cx - pcol));
-    const unsigned bal = __ballot_sync(kFull, start);
     int incl = newc;
 #pragma unroll
     for (int d = 1; d < 32; d <<= 1) {
         const int t = __shfl_up_sync(kFull, incl, d);
         if (lane >= d) incl += t;
     }
-    if (lane == 31) {
-        sm.wsum[warp] = __popc(bal);
-        sm.wcol[warp] = incl;
-    }
+    if (lane == 31) sm.wcol[warp] = incl;
     __syncthreads();
-    int sbefore = 0, stotal = 0, cbefore = 0, ncol = 0;
+    int cbefore = 0, ncol = 0;
 #pragma unroll
     for (int w = 0; w < kT / 32; ++w) {
-        const int x = sm.wsum[w], y = sm.wcol[w];
-        sbefore += w < warp ? x : 0;
+        const int y = sm.wcol[w];
         cbefore += w < warp ? y : 0;
-        stotal += x;
         ncol += y;
     }
     incl += cbefore;
@@ -395,15 +389,10 @@ __global__ void __launch_bounds__(TileCfg<D, V>::kTargets, TileCfg<D, V>::kMinBl
         }
     };
     constexpr int kCols = TileSmem<D, V>::kCols;
-    // One staging for the whole block when every window fits; otherwise per
-    // segment, in chunks (below).
+    // One staging for the whole block when every window fits; otherwise in
+    // chunks of columns (below).
     bool whole = ncol <= kCols;  // block-uniform
     if (whole) fill_columns(0, ncol);
-    if (start) {
-        const int g = sbefore + __popc(bal & ((1u << lane) - 1u));
-        sm.segc[g] = kwin;
-    }
-    if (tid == 0) sm.segc[stotal] = ncol;
     const int nx = P.g.nx;
     const int cy = D == 3 ? (valid ? row % nx : 0) : row, cz = D == 3 ? (valid ? row / nx : 0) : 0;
     const float px = me.x, py = me.y, pz = D == 3 ? me.z : 0.f;
@@ -456,28 +445,30 @@ __global__ void __launch_bounds__(TileCfg<D, V>::kTargets, TileCfg<D, V>::kMinBl
         if (whole && valid) evaluate(kwin, R * ncol);
     }
     if (!whole) {
-        // Per segment, in chunks of window columns [a, hi) serving the
-        // targets whose window starts in [a, hi - 3]; a chunk whose
-        // candidates do not fit is retried with half as many columns, and a
-        // single window that does not fit is read from global memory.
-        for (int g = 0; g < stotal; ++g) {
-            const int cb = sm.segc[g], ce = sm.segc[g + 1];
-            int a = cb, width = min(ce - cb, kCols);
-            while (a <= ce - 3) {
-                const int hi = min(a + width, ce);
-                fill_columns(a, hi);  // the previous staging no longer reads the columns
-                __syncthreads();
-                const bool staged = stage_columns<D, V>(A, P, cs, sm, hi - a);
-                const bool mine = valid && kwin >= a && kwin <= hi - 3;
-                if (staged) {
-                    if (mine) evaluate(kwin - a, R * (hi - a));
-                    a = hi - 2;
-                } else if (hi - a > 3) {
-                    width = max(3, (hi - a) / 2);
-                } else {
-                    if (mine) direct = true;  // computed after the loop, off the hot path
-                    a += 1;
-                }
+        // Chunks of the block's window columns [a, hi), each serving the
+        // targets whose window starts in [a, hi - 3].  A chunk may span
+        // segments: its columns are staged one by one with their own rows,
+        // and a window never leaves its segment.  A chunk whose candidates do
+        // not fit is retried with half as many columns (the width grows back
+        // after a success), and a single window that does not fit is read
+        // from global memory.  (Per-segment chunks served one segment per
+        // staging round: sparse 3D blocks spread over many grid rows.)
+        int a = 0, width = kCols;
+        while (a <= ncol - 3) {
+            const int hi = min(a + width, ncol);
+            fill_columns(a, hi);  // the previous staging no longer reads the columns
+            __syncthreads();
+            const bool staged = stage_columns<D, V>(A, P, cs, sm, hi - a);
+            const bool mine = valid && kwin >= a && kwin <= hi - 3;
+            if (staged) {
+                if (mine) evaluate(kwin - a, R * (hi - a));
+                a = hi - 2;
+                width = min(kCols, 2 * width);
+            } else if (hi - a > 3) {
+                width = max(3, (hi - a) / 2);
+            } else {
+                if (mine) direct = true;  // computed after the loop, off the hot path
+                a += 1;
             }
         }
     }
