@@ -299,6 +299,18 @@ int plg_set_use_graph(plg_ctx* ctx, int32_t on);
 #define PLG_K_FORCE 3   /* neighbour loop + integration + counting */
 #define PLG_K_COUNT 4
 
+/* Force kernel tile variant of this world (see PLG_TILE_VARIANTS below; 0
+ * by default).  Every variant gives the same bits. */
+int plg_set_tile(plg_ctx* ctx, int32_t variant);
+int plg_get_tile(plg_ctx* ctx, int32_t* variant);
+/* Times `steps` steps of every tile variant on the world as it is
+ * (restoring the particle state after each trial, so the world does not
+ * move), keeps the fastest and reports it in *chosen; ms_per_step (may be
+ * NULL) receives PLG_TILE_VARIANTS times.  Allocates a temporary copy of the
+ * state.  A world below 3 cells per axis has no tiles: *chosen is the
+ * current variant. */
+int plg_autotune(plg_ctx* ctx, int32_t steps, int32_t* chosen, double* ms_per_step);
+
 /* When on, steps run as plain launches bracketed by CUDA events on the
  * context's stream; plg_profile_read returns per-kernel totals since the
  * last enable.  Turning it on clears the totals. */
@@ -397,10 +409,11 @@ int plg_batch_get_stream(plg_batch* batch, void** stream);
 const char* plg_batch_last_error(plg_batch* batch);
 int plg_batch_step_stats(plg_batch* batch, int64_t* deferred);
 /* Force kernel tile variants (threads = targets per block, staging size):
- * 2D: 0 = 256 targets / 1536 staged candidates, 1 = 128 / 1024;
- * 3D: 0 = 128 / 1536, 1 = 64 / 1024.  Both give the same bits.  The
+ * 2D: 0 = 256 targets / 1536 staged candidates, 1 = 128 / 2560;
+ * 3D: 0 = 128 / 2048, 1 = 64 / 1024.  Both give the same bits.  The
  * cell size is not a tuning choice: it is rmax (the sorted order the
- * reference exposes depends on it). */
+ * reference exposes depends on it).  A single world has the same choice:
+ * plg_set_tile / plg_autotune. */
 #define PLG_TILE_VARIANTS 2
 int plg_batch_set_tile(plg_batch* batch, int32_t variant);
 int plg_batch_get_tile(plg_batch* batch, int32_t* variant);

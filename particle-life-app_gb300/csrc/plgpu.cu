@@ -194,6 +194,7 @@ struct plg_ctx {
 
     // graph of one step
     bool use_graph = true;
+    int variant = 0;  // force kernel tile variant (plg_set_tile / plg_autotune)
     cudaGraphExec_t gexec = nullptr;
     bool graph_dirty = true;
 
@@ -311,7 +312,7 @@ void enqueue_body(plg_ctx* c, const DebugOut* dbg, int32_t* cell_sorted, const H
     k1(PLG_K_GATHER);
     k0(PLG_K_FORCE);
     launch_force<D>(st, c->fp, c->general, buf_b<D>(c), c->cstart, c->slot_cell, buf_a<D>(c), c->cell, c->counts,
-                    c->defer, dbg, 0, snap);
+                    c->defer, dbg, c->variant, snap);
     k1(PLG_K_FORCE);
 }
 
@@ -1193,6 +1194,96 @@ int plg_set_use_graph(plg_ctx* c, int32_t on) {
     if (!c) return PLG_E_INVALID_ARG;
     c->use_graph = on != 0;
     return PLG_OK;
+}
+
+int plg_set_tile(plg_ctx* c, int32_t variant) {
+    if (!c) return PLG_E_INVALID_ARG;
+    if (variant < 0 || variant >= PLG_TILE_VARIANTS) return set_err(c, PLG_E_INVALID_ARG, "unknown tile variant");
+    if (variant != c->variant) c->graph_dirty = true;
+    c->variant = variant;
+    return PLG_OK;
+}
+
+int plg_get_tile(plg_ctx* c, int32_t* variant) {
+    if (!c || !variant) return PLG_E_INVALID_ARG;
+    *variant = c->variant;
+    return PLG_OK;
+}
+
+// Times `steps` steps of each tile variant on the world as it is, restoring
+// the particle state (A, the next cells and their counts) after each trial,
+// and keeps the fastest variant.  The trials allocate a copy of the state
+// and free it before returning.
+int plg_autotune(plg_ctx* c, int32_t steps, int32_t* chosen, double* ms_per_step) {
+    int rc = check_ready(c);
+    if (rc) return rc;
+    if (steps < 1) return set_err(c, PLG_E_INVALID_ARG, "autotune needs at least one step");
+    DeviceGuard g(c->device);
+    cudaStream_t st = c->stream;
+    if (c->n == 0 || c->general) {  // nothing to time / the literal kernel has no tiles
+        if (chosen) *chosen = c->variant;
+        return PLG_OK;
+    }
+    if ((rc = enqueue_rebin(c))) return rc;
+    const size_t n = (size_t)c->n, nc = (size_t)c->ncells;
+    const size_t vel_sz = c->dim == 2 ? sizeof(float2) : sizeof(float4);
+    const size_t bytes[4] = {sizeof(float4) * n, vel_sz * n, 4 * n, 4 * nc};
+    void* live[4] = {c->apt, c->avel, c->cell, c->counts};
+    void* save[4] = {};
+    for (int k = 0; k < 4 && !rc; ++k)
+        if (cudaMalloc(&save[k], bytes[k]) != cudaSuccess) {
+            cudaGetLastError();
+            rc = set_err(c, PLG_E_NO_MEMORY, "cudaMalloc (autotune state copy)");
+        }
+    auto copy_all = [&](bool restore) -> cudaError_t {
+        for (int k = 0; k < 4; ++k) {
+            cudaError_t e = cudaMemcpyAsync(restore ? live[k] : save[k], restore ? save[k] : live[k], bytes[k],
+                                            cudaMemcpyDeviceToDevice, st);
+            if (e != cudaSuccess) return e;
+        }
+        return cudaSuccess;
+    };
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (!rc && (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)) {
+        cudaGetLastError();
+        rc = set_err(c, PLG_E_CUDA, "cudaEventCreate (autotune)");
+    }
+    if (!rc && copy_all(false) != cudaSuccess) rc = cuda_fail(c, "autotune save", cudaGetLastError());
+    const int old = c->variant;
+    double best = 1e300;
+    int best_v = old;
+    for (int v = 0; v < PLG_TILE_VARIANTS && !rc; ++v) {
+        if (v != c->variant) c->graph_dirty = true;
+        c->variant = v;
+        if ((rc = enqueue_step(c))) break;  // builds the graph, untimed
+        if (cudaEventRecord(e0, st) != cudaSuccess) rc = cuda_fail(c, "autotune timing", cudaGetLastError());
+        for (int32_t k = 0; k < steps && !rc; ++k) rc = enqueue_step(c);
+        if (rc) break;
+        float ms = 0.f;
+        if (cudaEventRecord(e1, st) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
+            cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) {
+            rc = cuda_fail(c, "autotune timing", cudaGetLastError());
+            break;
+        }
+        const double per = ms / steps;
+        if (ms_per_step) ms_per_step[v] = per;
+        if (per < best) {
+            best = per;
+            best_v = v;
+        }
+        if (copy_all(true) != cudaSuccess) rc = cuda_fail(c, "autotune restore", cudaGetLastError());
+    }
+    if (!rc) rc = wait_stream(c, 0);
+    if (!rc) rc = read_status(c);
+    const int keep = rc ? old : best_v;
+    if (keep != c->variant) c->graph_dirty = true;
+    c->variant = keep;
+    for (void* p : save)
+        if (p) cudaFree(p);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (!rc && chosen) *chosen = keep;
+    return rc;
 }
 
 int plg_profile_enable(plg_ctx* c, int32_t on) {

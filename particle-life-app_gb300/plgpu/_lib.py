@@ -143,6 +143,9 @@ SIGNATURES = {
     "plg_download": (C.c_int, [_P, _DP, _DP, _I32P, _I32P]),
     "plg_step_download": (C.c_int, [_P, C.c_int32, _DP, _DP, _I32P, _I32P]),
     "plg_step_download_fuses": (C.c_int, [_P, _DP, _DP, _I32P, _I32P, C.POINTER(C.c_int32)]),
+    "plg_set_tile": (C.c_int, [_P, C.c_int32]),
+    "plg_get_tile": (C.c_int, [_P, C.POINTER(C.c_int32)]),
+    "plg_autotune": (C.c_int, [_P, C.c_int32, C.POINTER(C.c_int32), _DP]),
     "plg_particle_count": (C.c_int, [_P, _I64P]),
     "plg_request_stop": (C.c_int, [_P]),
     "plg_last_error": (C.c_char_p, [_P]),

@@ -318,6 +318,24 @@ class GpuWorld:
         )
         return pos, vel, types, ids
 
+    def set_tile(self, variant: int) -> None:
+        self._c(self.lib.plg_set_tile(self.ctx, int(variant)), "plg_set_tile")
+
+    def tile(self) -> int:
+        v = _lib.C.c_int32()
+        self._c(self.lib.plg_get_tile(self.ctx, _lib.C.byref(v)), "plg_get_tile")
+        return v.value
+
+    def autotune(self, steps: int = 5):
+        """Times every force tile variant on the world as it is (the state is
+        restored) and keeps the fastest; returns (variant, ms per step of
+        each)."""
+        chosen = _lib.C.c_int32()
+        ms = np.zeros(_lib.PLG_TILE_VARIANTS, np.float64)
+        self._c(self.lib.plg_autotune(self.ctx, int(steps), _lib.C.byref(chosen), _lib.ptr(ms, _lib.C.c_double)),
+                "plg_autotune")
+        return chosen.value, [float(x) for x in ms]
+
     def debug_step(self):
         """One step with the instrumented kernel: per-particle cell, pair
         count, pair hashes, FP32 accelerations (cell-sorted order)."""
