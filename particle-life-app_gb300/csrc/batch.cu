@@ -724,6 +724,7 @@ int plg_batch_autotune(plg_batch* b, int32_t steps, int32_t* chosen, double* ms_
     if (!rc && copy_all(false) != cudaSuccess) rc = bcuda(b, "autotune save", cudaGetLastError());
     const int old = b->variant;
     double best = 1e300;
+    double times[PLG_TILE_VARIANTS] = {};
     int best_v = old;
     for (int v = 0; v < PLG_TILE_VARIANTS && !rc; ++v) {
         if (v != b->variant) destroy_batch_graph(b);
@@ -740,6 +741,7 @@ int plg_batch_autotune(plg_batch* b, int32_t steps, int32_t* chosen, double* ms_
         }
         const double per = ms / steps;
         if (ms_per_step) ms_per_step[v] = per;
+        times[v] = per;
         if (per < best) {
             best = per;
             best_v = v;
@@ -756,6 +758,7 @@ int plg_batch_autotune(plg_batch* b, int32_t steps, int32_t* chosen, double* ms_
         destroy_batch_graph(b);
         return rc;
     }
+    best_v = switch_if_faster(old, best_v, times);
     if (best_v != b->variant) destroy_batch_graph(b);
     b->variant = best_v;
     if (chosen) *chosen = best_v;

@@ -322,6 +322,13 @@ void launch_force_batch(cudaStream_t st, const ForceParams* worlds, const int* w
 // Counts every positive steps_left[k] (k < nworlds) down by one.
 void launch_batch_tick(cudaStream_t st, int* steps_left, int nworlds);
 
+// The autotuners' choice: the fastest variant `best` replaces the current
+// one only when it is at least 2% faster, so timing noise between nearly
+// equal variants does not flip the choice.
+inline int switch_if_faster(int current, int best, const double* ms_per_step) {
+    return ms_per_step[best] < 0.98 * ms_per_step[current] ? best : current;
+}
+
 // Targets per block of the force kernel's tile variant.
 int tile_targets(int dim, int variant);
 

@@ -1251,6 +1251,7 @@ int plg_autotune(plg_ctx* c, int32_t steps, int32_t* chosen, double* ms_per_step
     if (!rc && copy_all(false) != cudaSuccess) rc = cuda_fail(c, "autotune save", cudaGetLastError());
     const int old = c->variant;
     double best = 1e300;
+    double times[PLG_TILE_VARIANTS] = {};
     int best_v = old;
     for (int v = 0; v < PLG_TILE_VARIANTS && !rc; ++v) {
         if (v != c->variant) c->graph_dirty = true;
@@ -1267,6 +1268,7 @@ int plg_autotune(plg_ctx* c, int32_t steps, int32_t* chosen, double* ms_per_step
         }
         const double per = ms / steps;
         if (ms_per_step) ms_per_step[v] = per;
+        times[v] = per;
         if (per < best) {
             best = per;
             best_v = v;
@@ -1275,7 +1277,7 @@ int plg_autotune(plg_ctx* c, int32_t steps, int32_t* chosen, double* ms_per_step
     }
     if (!rc) rc = wait_stream(c, 0);
     if (!rc) rc = read_status(c);
-    const int keep = rc ? old : best_v;
+    const int keep = rc ? old : switch_if_faster(old, best_v, times);
     if (keep != c->variant) c->graph_dirty = true;
     c->variant = keep;
     for (void* p : save)

@@ -67,7 +67,9 @@ def test_autotune_restores_the_world(gpu, case):
         assert chosen in range(_lib.PLG_TILE_VARIANTS)
         assert a.tile() == chosen
         assert len(ms) == _lib.PLG_TILE_VARIANTS and all(t > 0 for t in ms)
-        assert ms[chosen] == min(ms)
+        fastest = int(np.argmin(ms))
+        # the fastest variant replaces the current one (0) only when it is at least 2% faster
+        assert chosen == (fastest if ms[fastest] < 0.98 * ms[0] else 0)
         for x, y in zip(a.download(), b.download()):
             assert np.array_equal(x, y)
         a.step(2)
