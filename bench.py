@@ -22,7 +22,8 @@ Our arm (default):
   batched  512 uneven 2D worlds through plg_batch_* (autotuned) against the
          same worlds one at a time through single-world contexts.
   serving  Poisson request arrivals through plg_server_* (scaled sizes, see
-         run_serving), completion latency p50/p99 and delivered throughput.
+         run_serving), completion latency p50/p99 and delivered throughput,
+         against a sample of the same requests run one at a time.
 --impl reference: the same workload through the oracle port on all host
 cores (the reference is Java and no JDK exists on either machine).
 
@@ -126,6 +127,8 @@ def parse(argv=None):
     ap.add_argument("--steps-3d", type=int, default=20)
     ap.add_argument("--serve-seconds", type=float, default=10.0)
     ap.add_argument("--serve-rate", type=float, default=200.0)
+    ap.add_argument("--serve-alone-s", type=float, default=3.0,
+                    help="seconds of one-at-a-time stepping for the serving comparison")
     return ap.parse_args(argv)
 
 
@@ -348,10 +351,35 @@ def run_serving(args) -> dict:
     for rid in ids:
         srv.result(rid)
     srv.close()
+    # The same requests one at a time, each alone in a single-world context
+    # (plg_step of its whole step count; only the steps are timed), in
+    # arrival order until about --serve-alone-s seconds of stepping.
+    from plgpu.physics import GpuWorld
+
+    alone_ps, alone_s, alone_n = 0, 0.0, 0
+    for dim, w, steps in reqs:
+        g = GpuWorld(dim, w.pos.shape[0])
+        g.set_settings(w.rmax, w.friction, w.force, w.dt, beta=w.beta, wrap=w.wrap)
+        g.set_matrix(w.matrix)
+        g.upload(w.pos, w.vel, w.types)
+        t1 = time.perf_counter()
+        g.step(steps)
+        alone_s += time.perf_counter() - t1
+        g.close()
+        alone_ps += w.pos.shape[0] * steps
+        alone_n += 1
+        if alone_s >= args.serve_alone_s:
+            break
+    alone = alone_ps / alone_s
+    served = st["particle_steps"] / wall
     return {"metric": "served requests: completion latency and aggregate particle-steps/s",
             "requests": count, "completed": st["completed"], "latency_p50_ms": st["latency_p50_ms"],
             "latency_p99_ms": st["latency_p99_ms"], "latency_mean_ms": st["latency_mean_ms"],
-            "value": st["particle_steps"] / wall, "unit": UNIT, "offered_particle_steps_per_s": offered,
+            "value": served, "unit": UNIT, "offered_particle_steps_per_s": offered,
+            "one_at_a_time": {"value": alone, "unit": UNIT, "requests": alone_n,
+                              "how": "the first requests in arrival order, each in its own context, plg_step of its "
+                                     "step count, steps timed alone (host wall clock)"},
+            "speedup_vs_one_at_a_time": served / alone,
             "wall_s": wall, "peak_resident_bytes": st["peak_resident_bytes"],
             "config": f"Poisson arrivals {args.serve_rate:g}/s for {args.serve_seconds:g} s, 2D/3D 50/50, "
                       "N log-uniform [1e3, 2e5], types 3..16, k U[10, 50], steps U[100, 1000], budget 150 GB, "
