@@ -660,20 +660,25 @@ class Physics:
             self._host_dirty = False
 
     def update(self) -> None:
-        """One Physics.update() on the GPU."""
+        """One Physics.update() on the GPU.  With sync_policy 'every' the
+        host arrays come back in the same call (plg_step_download: the step's
+        force kernel writes them)."""
         self._push()
-        self.world.step(1)
-        self._device_newer = True
         if self.sync_policy == "every":
-            self._sync_host()
+            self._take(*self.world.step_download(1))
+        else:
+            self.world.step(1)
+            self._device_newer = True
+
+    def _take(self, pos, vel, types, ids) -> None:
+        self.positions, self.velocities, self.types = pos, vel, types
+        self.ids = self._device_ids[ids]
+        self._device_newer = False
 
     def _sync_host(self) -> None:
         if not self._device_newer or self._world is None:
             return
-        pos, vel, types, ids = self._world.download()
-        self.positions, self.velocities, self.types = pos, vel, types
-        self.ids = self._device_ids[ids]
-        self._device_newer = False
+        self._take(*self._world.download())
 
     def sync_host(self) -> None:
         """Brings the host arrays up to date (for sync_policy='manual')."""

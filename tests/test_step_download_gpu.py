@@ -179,3 +179,23 @@ def test_step_download_errors_and_stop(gpu):
             assert np.array_equal(x, y)
     finally:
         w.close()
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_host_mirror_sync_policies_agree(gpu, dim):
+    """Physics.update() with sync_policy 'every' (plg_step_download each
+    update) and 'manual' (plain steps, one read-back at the end) leave the
+    same host arrays, ids included."""
+    from plgpu import ParticleLifeAccelerator, Physics
+
+    runs = []
+    for policy in ("every", "manual"):
+        p = Physics(ParticleLifeAccelerator(), dim=dim, seed=11, initial_count=30_000, sync_policy=policy)
+        p.settings.rmax = 0.02 if dim == 2 else 0.05
+        for _ in range(4):
+            p.update()
+        p.sync_host()
+        runs.append((p.positions.copy(), p.velocities.copy(), p.types.copy(), p.ids.copy()))
+        p.close()
+    for a, b in zip(*runs):
+        assert np.array_equal(a, b)
