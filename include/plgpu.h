@@ -409,7 +409,7 @@ int plg_batch_get_stream(plg_batch* batch, void** stream);
 const char* plg_batch_last_error(plg_batch* batch);
 int plg_batch_step_stats(plg_batch* batch, int64_t* deferred);
 /* Force kernel tile variants (threads = targets per block, staging size):
- * 2D: 0 = 256 targets / 1536 staged candidates, 1 = 128 / 2560;
+ * 2D: 0 = 128 targets / 1024 staged candidates, 1 = 128 / 2560;
  * 3D: 0 = 128 / 2048, 1 = 64 / 1024.  Both give the same bits.  The
  * cell size is not a tuning choice: it is rmax (the sorted order the
  * reference exposes depends on it).  A single world has the same choice:

@@ -8,8 +8,8 @@
 // and, in its epilogue, the counting pass of the next makeContainers
 // (Physics.java:328-332) on the new position.
 //
-// Tiling.  A block takes 256 (3D: 128) consecutive targets of the sorted
-// order, one thread each; their cells come from the sort.  The cells are
+// Tiling.  A block takes 128 consecutive targets of the sorted order (tile
+// variant 0), one thread each; their cells come from the sort.  The cells are
 // nondecreasing, so the targets fall into a few "segments" (targets of one
 // grid row: one y in 2D, one (y, z) in 3D).  A target in column cx needs the
 // window of columns cx-1..cx+1 over its R stencil rows (3 in 2D, 9 in 3D);
@@ -19,8 +19,8 @@
 // windows fit, one staging serves every target; otherwise the block's
 // columns are staged in chunks (which may span segments), halved until they
 // fit, and a single window that still does not fit (a very dense region) is
-// read from global memory
-// in the same candidate order (direct_stencil), giving the same bits.  The
+// read from global memory in the same candidate order (direct_stencil),
+// giving the same bits.  The
 // candidate loop is branch-free FP32.  A target that meets a candidate
 // needing the FP64 decision is deferred: its warp recomputes it from global
 // memory at the end (fixup_target).
@@ -133,16 +133,18 @@ __global__ void __launch_bounds__(kThreads) k_force_general(const __grid_constan
 //               blocks with spilled registers measured slower)
 //   kCap        staged candidates per staging
 //   kCells      stencil cells per staging (R x columns)
-// 2D: variant 0 suits the 1M-particle world (a few cells per tile); variant
-// 1 (half the targets, a staging for 2560 candidates) suits very dense worlds
-// (hundreds of particles per cell), where variant 0's windows overflow; it
-// won the autotuner on the batched benchmark (6.24 vs 6.33 ms per step).
+// 2D: variant 0 suits the 1M-particle world (a few cells per tile): 8
+// blocks of 128 targets per SM overlap one block's latency-bound prologue
+// and epilogue with the others' candidate loops better than 4 blocks of
+// 256 (93 vs 95 us per launch, the same 64 registers); variant 1 (fewer
+// blocks, a staging for 2560 candidates) suits very dense worlds (hundreds
+// of particles per cell), where variant 0's windows overflow.
 // 3D: variant 1 is the smaller tile for sparse worlds.
 template <int D, int V>
 struct TileCfg;
 template <>
 struct TileCfg<2, 0> {
-    static constexpr int kTargets = 256, kMinBlocks = 4, kCap = 1536, kCells = 512;
+    static constexpr int kTargets = 128, kMinBlocks = 8, kCap = 1024, kCells = 256;
 };
 template <>
 struct TileCfg<2, 1> {
@@ -157,7 +159,7 @@ struct TileCfg<3, 1> {
     static constexpr int kTargets = 64, kMinBlocks = 10, kCap = 1024, kCells = 384;
 };
 
-// Lives in dynamic shared memory (variant 0: about 35 KB in 2D, 41 KB in 3D).
+// Lives in dynamic shared memory (variant 0: about 21 KB in 2D, 39 KB in 3D).
 // Staged columns: the sorted union of the windows cx-1..cx+1 of the staged
 // targets, as "virtual" columns -1..nx (-1 and nx being the periodic images
 // of columns nx-1 and 0), each with the grid row of its segment.
@@ -278,10 +280,10 @@ __device__ __forceinline__ bool stage_columns(const ForceArgs<D>& A, const Force
 
 
 
-// Main force kernel (nx >= 3): one thread per target; a block takes 256 (3D:
-// 128) consecutive targets, stages their windows so that each target reads
-// one contiguous run (or, where a window does not fit, reads the same cells
-// from global memory).  Neighbouring threads mostly share a cell, hence a
+// Main force kernel (nx >= 3): one thread per target; a block takes
+// kTargets (128 in variant 0) consecutive targets and stages their windows
+// so that each target reads one contiguous run (or, where a window does not
+// fit, reads the same cells from global memory).  Neighbouring threads mostly share a cell, hence a
 // window, so their candidate loads are broadcasts.  FP32 only: a target
 // whose neighbourhood holds a candidate that needs the FP64 decision is
 // deferred to its warp's closing pass (fixup_target), which recomputes it
