@@ -118,6 +118,12 @@ def test_null_context_calls_fail_cleanly(lib):
     assert lib.plg_step(None, 1) == _lib.PLG_E_INVALID_ARG
     assert lib.plg_request_stop(None) == _lib.PLG_E_INVALID_ARG
     assert lib.plg_last_error(None) == b"null context"
+    assert lib.plg_step_download(None, 1, None, None, None, None) == _lib.PLG_E_INVALID_ARG
+    f = C.c_int32(-1)
+    assert lib.plg_step_download_fuses(None, None, None, None, None, C.byref(f)) == _lib.PLG_E_INVALID_ARG
+    assert lib.plg_set_tile(None, 0) == _lib.PLG_E_INVALID_ARG
+    assert lib.plg_get_tile(None, C.byref(f)) == _lib.PLG_E_INVALID_ARG
+    assert lib.plg_autotune(None, 2, C.byref(f), None) == _lib.PLG_E_INVALID_ARG
     out = C.c_void_p()
     assert lib.plg_create(5, 10, C.byref(out)) == _lib.PLG_E_INVALID_ARG
     assert lib.plg_create(2, 0, C.byref(out)) == _lib.PLG_E_INVALID_ARG
