@@ -1,4 +1,4 @@
-// force_common.cuh — the building blocks of the force kernels (k_force.cu):
+// force_common.cuh — the building blocks of the force kernels (force_tile.cuh):
 // kernel arguments, the FP64 pair decision and term, the candidate
 // evaluation over a staged window, the global-memory stencils (the direct
 // path and the deferred FP64 pass) and the epilogue.  Every path evaluates a
