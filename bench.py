@@ -13,7 +13,8 @@ Our arm (default):
   e2e    the public API with host buffers: per step plg_upload (pinned host
          double/int arrays) + plg_step_download (one step whose force kernel
          writes the snapshot to the host arrays), host wall clock; "unfused"
-         beside it: plg_upload + plg_step + plg_download.
+         beside it: plg_upload + plg_step + plg_download; "host_link": the
+         link's DMA ceiling measured live and the calls' fractions of it.
   roofline of the dominant kernel (the force kernel), from per-kernel CUDA
          events over a profiled pass of the same steps.
   cpu_baseline  the oracle (C FP64 restatement of the reference's step, all
@@ -311,6 +312,29 @@ def run_blobs_3d(args) -> dict:
                       f"rmax {w.rmax} (mean 40 neighbours), dt 0.01; seeded Philox"}
 
 
+def host_link(dev, nbytes: int = 64 << 20, reps: int = 5) -> dict:
+    """The host link's DMA ceiling each way: a page-locked host buffer of
+    `nbytes` copied to and from the device, median over `reps` copies timed
+    with CUDA events (the ceiling the e2e leg's transfers are held to)."""
+    import torch
+
+    h = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
+    d = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+    out = {"bytes": nbytes}
+    for key, dst, src in (("h2d_gbs", d, h), ("d2h_gbs", h, d)):
+        ts = []
+        for k in range(reps + 1):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            dst.copy_(src, non_blocking=True)
+            b.record()
+            b.synchronize()
+            if k:
+                ts.append(a.elapsed_time(b))
+        out[key] = nbytes / (float(np.median(ts)) * 1e-3) / 1e9
+    return out
+
+
 def plgpu_check(status, ctx, what):
     import plgpu.physics
 
@@ -529,6 +553,16 @@ def run_ours(args):
     unfused_value = reps.rate(n * args.e2e_steps, e2e_s, dev)
     fused_s = reps.max_over_ranks(fused_s, dev)
     e2e_value = reps.rate(n * args.e2e_steps, fused_s, dev)
+    link = host_link(dev)
+    up_ms, sd_ms = (1e3 * x / args.e2e_steps for x in fparts)
+    h2d, d2h = n * (24 + 24 + 4), n * (24 + 24 + 4 + 4)
+    link.update({
+        "upload_gbs": h2d / (up_ms * 1e-3) / 1e9, "upload_frac": h2d / (up_ms * 1e-3) / 1e9 / link["h2d_gbs"],
+        "stepdownload_gbs": d2h / (sd_ms * 1e-3) / 1e9,
+        "stepdownload_frac": d2h / (sd_ms * 1e-3) / 1e9 / link["d2h_gbs"],
+        "floor_ms": 1e3 * (h2d / (link["h2d_gbs"] * 1e9) + d2h / (link["d2h_gbs"] * 1e9)),
+        "note": "rates are whole-call wall clock (the step-download call includes the sort and the force "
+                "arithmetic); floor_ms = the bytes of one step at the DMA ceilings"})
 
     deferred = w.deferred()
     # pair statistics of the current state (one instrumented step)
@@ -605,7 +639,7 @@ def run_ours(args):
                     "d2h_bytes_per_step": n * (24 + 24 + 4 + 4), "steps": args.e2e_steps,
                     "api": "plg_upload + plg_step_download (the force kernel writes the snapshot), pinned host "
                            "buffers, host wall clock",
-                    "snapshot_fused": bool(fuses.value),
+                    "snapshot_fused": bool(fuses.value), "host_link": link,
                     "ms_upload_stepdownload": [round(1e3 * x / args.e2e_steps, 4) for x in fparts],
                     "unfused": {"value": unfused_value, "api": "plg_upload + plg_step + plg_download",
                                 "ms_upload_step_download": [round(1e3 * x / args.e2e_steps, 4) for x in parts]}},
