@@ -343,6 +343,14 @@ int plg_step_stats(plg_ctx* ctx, int64_t* deferred);
  * TFLOP/s (an FFMA counts 2 flops).  Runs for about 0.1 s. */
 int plg_probe_fp32_peak(double* tflops);
 
+/* Test hook for the bounded device waits: runs the step's scan kernel on a
+ * private two-tile problem where its look-back wait can never be satisfied,
+ * so the wait runs out (about 0.3 to 3 s), the kernel raises its error word
+ * and returns, and the context stays usable.  *status receives the kernel's
+ * error word (bit 3: a bounded wait ran out), *seconds (may be NULL) the
+ * kernel's duration.  Uses the current device. */
+int plg_test_scan_wait(uint32_t* status, double* seconds);
+
 /* ---- batched worlds ---------------------------------------------------- */
 
 /* Many independent worlds advanced together: one step launch sorts and

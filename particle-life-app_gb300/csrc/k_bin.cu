@@ -15,6 +15,7 @@
 // stable re-rank costs sum_c n_c^2 compares, a ninth of the force loop's
 // sum_c n_c * (9 neighbour cells) candidate tests.
 #include "plg_internal.cuh"
+#include "plgpu.h"
 
 namespace plg {
 
@@ -504,3 +505,48 @@ template void launch_gather<3>(cudaStream_t, int, const uint32_t*, const uint32_
                                StateBuf<3>, int32_t*);
 
 }  // namespace plg
+
+// Test hook: the scan's bounded look-back wait runs out on purpose.  One
+// block over a two-tile problem whose tile counter starts at 1 takes tile 1
+// and waits for tile 0's status word, which no block publishes; after
+// kLookbackSpinLimit polls it raises kDevSpinLimit, treats the missing
+// prefix as 0 and finishes, so the kernel returns and the context stays
+// usable.  Every access stays inside the buffers allocated here.
+extern "C" int plg_test_scan_wait(uint32_t* status_out, double* seconds) {
+    using namespace plg;
+    if (!status_out) return PLG_E_INVALID_ARG;
+    const int ncells = 2 * kScanTile;
+    uint32_t *counts = nullptr, *cstart = nullptr, *status = nullptr;
+    unsigned long long* state = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    int rc = PLG_OK;
+    auto ok = [&](cudaError_t e) {
+        if (e != cudaSuccess && rc == PLG_OK) {
+            cudaGetLastError();
+            rc = e == cudaErrorMemoryAllocation ? PLG_E_NO_MEMORY : PLG_E_CUDA;
+        }
+        return rc == PLG_OK;
+    };
+    const unsigned long long first_tile = 1;
+    if (ok(cudaMalloc(&counts, sizeof(uint32_t) * ncells)) &&
+        ok(cudaMalloc(&cstart, sizeof(uint32_t) * (ncells + 1))) && ok(cudaMalloc(&status, sizeof(uint32_t))) &&
+        ok(cudaMalloc(&state, sizeof(unsigned long long) * 3)) &&
+        ok(cudaMemset(counts, 0, sizeof(uint32_t) * ncells)) && ok(cudaMemset(status, 0, sizeof(uint32_t))) &&
+        ok(cudaMemset(state, 0, sizeof(unsigned long long) * 3)) &&
+        ok(cudaMemcpy(state, &first_tile, sizeof(first_tile), cudaMemcpyHostToDevice)) &&
+        ok(cudaEventCreate(&e0)) && ok(cudaEventCreate(&e1)) && ok(cudaEventRecord(e0))) {
+        k_scan<<<1, kScanThreads>>>(counts, ncells, cstart, state, status, nullptr);
+        if (ok(cudaGetLastError()) && ok(cudaEventRecord(e1)) && ok(cudaEventSynchronize(e1)) &&
+            ok(cudaMemcpy(status_out, status, sizeof(uint32_t), cudaMemcpyDeviceToHost))) {
+            float ms = 0.f;
+            if (seconds && ok(cudaEventElapsedTime(&ms, e0, e1))) *seconds = 1e-3 * ms;
+        }
+    }
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    cudaFree(counts);
+    cudaFree(cstart);
+    cudaFree(status);
+    cudaFree(state);
+    return rc;
+}

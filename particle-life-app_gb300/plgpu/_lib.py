@@ -146,6 +146,7 @@ SIGNATURES = {
     "plg_set_tile": (C.c_int, [_P, C.c_int32]),
     "plg_get_tile": (C.c_int, [_P, C.POINTER(C.c_int32)]),
     "plg_autotune": (C.c_int, [_P, C.c_int32, C.POINTER(C.c_int32), _DP]),
+    "plg_test_scan_wait": (C.c_int, [C.POINTER(C.c_uint32), _DP]),
     "plg_particle_count": (C.c_int, [_P, _I64P]),
     "plg_request_stop": (C.c_int, [_P]),
     "plg_last_error": (C.c_char_p, [_P]),
