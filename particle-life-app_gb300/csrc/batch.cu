@@ -568,6 +568,7 @@ int plg_batch_destroy(plg_batch* b) {
 
 int plg_batch_update(plg_batch* b, int32_t nremove, const int32_t* remove_ids, int32_t nadd,
                      const plg_world_desc* add, int32_t* ids_out) {
+    const TraceRange tr("plg_batch_update");
     if (!b) return PLG_E_INVALID_ARG;
     if (nremove < 0 || nadd < 0) return berr(b, PLG_E_INVALID_ARG, "negative world count");
     if ((nremove > 0 && !remove_ids) || (nadd > 0 && !add)) return berr(b, PLG_E_INVALID_ARG, "NULL world list");
@@ -629,6 +630,7 @@ int plg_batch_sync(plg_batch* b, double timeout_s) {
 }
 
 int plg_batch_step(plg_batch* b, int32_t nsteps) {
+    const TraceRange tr("plg_batch_step");
     const int rc = plg_batch_step_async(b, nsteps);
     if (rc) return rc;
     return plg_batch_sync(b, 0.0);

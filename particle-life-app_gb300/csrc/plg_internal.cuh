@@ -11,9 +11,19 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 #include <stdint.h>
 
 namespace plg {
+
+// NVTX range over a public call (plg_step, plg_upload, ...), so that a
+// profiler can select its kernels (ncu --nvtx); free when no tool is attached.
+struct TraceRange {
+    explicit TraceRange(const char* name) { nvtxRangePushA(name); }
+    ~TraceRange() { nvtxRangePop(); }
+    TraceRange(const TraceRange&) = delete;
+    TraceRange& operator=(const TraceRange&) = delete;
+};
 
 constexpr unsigned kFull = 0xffffffffu;
 

@@ -633,6 +633,7 @@ int plg_set_matrix(plg_ctx* c, int32_t n, const double* m) {
 }
 
 int plg_upload(plg_ctx* c, int64_t n, const double* pos, const double* vel, const int32_t* type) {
+    const TraceRange tr("plg_upload");
     if (!c) return PLG_E_INVALID_ARG;
     if (n < 0) return set_err(c, PLG_E_INVALID_ARG, "negative particle count");
     if (n > c->cap) return set_err(c, PLG_E_CAPACITY, "more particles than the context capacity");
@@ -717,6 +718,7 @@ int plg_sync(plg_ctx* c, double timeout_s) {
 }
 
 int plg_step(plg_ctx* c, int32_t nsteps) {
+    const TraceRange tr("plg_step");
     int rc = plg_step_async(c, nsteps);
     if (rc == PLG_E_STOPPED) {
         std::string m = c->err;
@@ -730,6 +732,7 @@ int plg_step(plg_ctx* c, int32_t nsteps) {
 }
 
 int plg_download(plg_ctx* c, double* pos, double* vel, int32_t* type, int32_t* id) {
+    const TraceRange tr("plg_download");
     if (!c) return PLG_E_INVALID_ARG;
     if (!c->state_valid) return set_err(c, PLG_E_STATE, "no valid particle state: call plg_upload");
     DeviceGuard g(c->device);
@@ -779,6 +782,7 @@ int plg_step_download_fuses(plg_ctx* c, const double* pos, const double* vel, co
 }
 
 int plg_step_download(plg_ctx* c, int32_t nsteps, double* pos, double* vel, int32_t* type, int32_t* id) {
+    const TraceRange tr("plg_step_download");
     int rc = check_ready(c);
     if (rc) return rc;
     if (nsteps < 0) return set_err(c, PLG_E_INVALID_ARG, "negative step count");
@@ -1221,6 +1225,7 @@ int plg_get_tile(plg_ctx* c, int32_t* variant) {
 // and keeps the fastest variant.  The trials allocate a copy of the state
 // and free it before returning.
 int plg_autotune(plg_ctx* c, int32_t steps, int32_t* chosen, double* ms_per_step) {
+    const TraceRange tr("plg_autotune");
     int rc = check_ready(c);
     if (rc) return rc;
     if (steps < 1) return set_err(c, PLG_E_INVALID_ARG, "autotune needs at least one step");

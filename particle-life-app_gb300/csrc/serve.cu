@@ -28,12 +28,19 @@
 #include <vector>
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include "plgpu.h"
 
 namespace {
 
 using Clock = std::chrono::steady_clock;
+
+// NVTX range over one scheduler chunk (free when no profiler is attached).
+struct ChunkRange {
+    ChunkRange() { nvtxRangePushA("plg_server chunk"); }
+    ~ChunkRange() { nvtxRangePop(); }
+};
 
 struct Request {
     int64_t id = 0;
@@ -233,6 +240,7 @@ void scheduler(plg_server* s) {
             continue;
         }
         const auto t0 = Clock::now();
+        const ChunkRange tr;
         for (int d = 0; d < 2; ++d)
             if (k[d] && plg_batch_step_async(s->batch[d], k[d]))
                 return (void)fail_server(s, PLG_E_CUDA, std::string("step: ") + plg_batch_last_error(s->batch[d]));
