@@ -365,43 +365,87 @@ __device__ __forceinline__ float4 shift_candidate(float4 q, float sx, float sy, 
     return q;
 }
 
-// rsqrt.approx.ftz.f32: the fast path only sees d2 >= 2^-100, a normal float.
+// rsqrt.approx.ftz.f32: a zero or subnormal d2 gives +inf.
 __device__ __forceinline__ float rsqrt_approx(float x) {
     float r;
     asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
     return r;
 }
 
+// x * y with subnormal inputs and results flushed to zero.
+__device__ __forceinline__ float mul_ftz(float x, float y) {
+    float r;
+    asm("mul.ftz.f32 %0, %1, %2;" : "=f"(r) : "f"(x), "f"(y));
+    return r;
+}
+
+// min(m, x) that returns NaN when either is NaN (a running minimum that
+// remembers a NaN once it has seen one).
+__device__ __forceinline__ float min_nan(float m, float x) {
+    float r;
+    asm("min.NaN.f32 %0, %1, %2;" : "=f"(r) : "f"(m), "f"(x));
+    return r;
+}
+
+// (qx - px, qy - py) as one packed FP32 subtraction (two lanes of one
+// instruction, each rounded like a scalar subtraction).
+__device__ __forceinline__ void sub_pair(float qx, float qy, float px, float py, float& dx, float& dy) {
+    unsigned long long q, p, d;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(q) : "f"(qx), "f"(qy));
+    asm("mov.b64 %0, {%1, %2};" : "=l"(p) : "f"(px), "f"(py));
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(q), "l"(p));
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(dx), "=f"(dy) : "l"(d));
+}
+
 // Loop constants of the candidate evaluation, read once into registers
 // (otherwise the compiler re-reads them from the parameter bank per
-// candidate).
-// The decision band as |d2 - mid| < half: lo, mid and hi are floats a few
-// ulp apart, so hi - lo, mid - lo and hi - mid are exact, mid lies in
-// [lo, hi], and (mid - half, mid + half) contains (lo, hi); for d2 within a
-// factor 2 of mid the subtraction d2 - mid is exact too, and any other d2 is
-// far outside.  brm2 = (beta rmax)^2: the repulsion branch tests d2, which
-// is ready before the rsqrt.
+// candidate).  lo: the FP32 d2 at or below which a pair certainly interacts
+// (the debug counts use it); uflag: the threshold of the |u| test below.
+//
+// A target whose running minimum of |u| ends below uflag, or is NaN, is
+// recomputed with the FP64 decisions.  Why that covers every pair the FP32
+// d2 cannot decide: with s = |d|/rmax, u = 1 - |1 + beta - 2 s| / (1 - beta)
+// is the Accelerator's triangle factor (app/Main.java:275-280), zero at
+// s = beta and at s = 1.  A pair in the FP32 decision band lo < d2 < hi (d2
+// within 2^-19 relative of rmax^2, kBandRel) has |s - 1| <= 2^-20 + 2^-24,
+// so its exact u has |u| <= 2.02e-6 / (1 - beta).  The FP32 u differs from
+// it by less than 0.87e-6 / (1 - beta): rsqrt.approx (relative error below
+// 2^-22) and the product give dist within 3e-7 relative, the fma for
+// t = 1 + beta - 2 dist / rmax adds its rounding and those of -2/rmax and
+// 1 + beta (|t| error < 8.3e-7 near s = 1), and the last fma scales it by
+// 1/(1 - beta).  So every band pair has |u| < 2.9e-6 / (1 - beta), and
+// uflag = 7e-6 / (1 - beta) keeps a factor 2.4 of margin.  A pair whose FP32
+// d2 is zero or subnormal (coincident or nearly coincident particles; the
+// reference keeps a pair whenever its FP64 d2 != 0) gives
+// dist = 0 * inf = NaN, which reaches the running minimum.  Every other pair
+// is decided correctly in FP32: d2 <= lo interacts, d2 >= hi does not and
+// has u < 0, hence an exact zero term.  A pair near s = beta may raise the
+// flag too; that costs a recomputation, never a wrong result.
 struct LoopK {
-    float lo, hi, tiny, m2, opb, iomb, k1, brm2, mid, half;
+    float lo, m2, opb, iomb, k1, uflag;
     __device__ __forceinline__ explicit LoopK(const ForceParams& P)
-        : lo(P.lo), hi(P.hi), tiny(P.tiny), m2(P.m2_inv_rmax), opb(P.one_plus_beta),
-          iomb(P.inv_one_minus_beta), k1(P.k1), brm2(P.beta_rmax * P.beta_rmax) {
-        mid = lo + (hi - lo) * 0.5f;
-        half = fmaxf(mid - lo, hi - mid);
-    }
+        : lo(P.lo), m2(P.m2_inv_rmax), opb(P.one_plus_beta), iomb(P.inv_one_minus_beta), k1(P.k1),
+          uflag(7e-6f * P.inv_one_minus_beta) {}
 };
 
 // One candidate: d = q - p with the image shifts already applied to q and p,
-// the FP32 Accelerator term added to acc; bmin / dmin keep the smallest
-// |d2 - mid| and d2 seen, from which the caller flags band and tiny pairs
-// (a running minimum costs fewer instructions than a flag per candidate).
-// The staged and the direct paths both use it, in the same candidate order,
-// so they produce the same bits.  Returns d2.
+// the FP32 Accelerator term added to acc, and umin = min(umin, |u|) (NaN
+// sticks).  The staged and the direct paths both use it, in the same
+// candidate order, so they produce the same bits.  Returns d2.
+//
+// Force law in FP32, with inv = 1/|d| (rsqrt.approx) and u+ = max(u, 0):
+//   below beta rmax   f/|d| = 1/(beta rmax) - 1/|d|   (u+ = 0 there)
+//   beta rmax..rmax   f/|d| = a u+ / |d|
+// both as g = fma(a u+ - 1, inv, min(k1, inv)), k1 = 1/(beta rmax):
+// below beta rmax inv > k1 and a u+ - 1 = -1, giving k1 - inv; above it
+// min(k1, inv) = inv, giving (a u+ - 1) inv + inv; beyond rmax (u+ = 0) that
+// is fma(-1, inv, inv) = +0 exactly, so a candidate beyond rmax adds an exact
+// zero and needs no select.
 template <int D>
 __device__ __forceinline__ float eval_candidate(const LoopK& K, float qx, float qy, float qz, float pxe, float pye,
-                                                float pze, float a, Acc& acc, float& bmin, float& dmin) {
-    const float dx = qx - pxe;
-    const float dy = qy - pye;
+                                                float pze, float a, Acc& acc, float& umin) {
+    float dx, dy;
+    sub_pair(qx, qy, pxe, pye, dx, dy);
     float d2;
     float dz = 0.f;
     if (D == 3) {
@@ -410,18 +454,21 @@ __device__ __forceinline__ float eval_candidate(const LoopK& K, float qx, float 
     } else {
         d2 = fmaf(dx, dx, dy * dy);
     }
-    bmin = fminf(bmin, fabsf(d2 - K.mid));
-    dmin = fminf(dmin, d2);
     const float inv = rsqrt_approx(d2);
-    const float dist = d2 * inv;
+    const float dist = mul_ftz(d2, inv);
     const float t = fmaf(dist, K.m2, K.opb);
-    const float u = fmaxf(fmaf(-fabsf(t), K.iomb, 1.f), 0.f);
-    const float g = d2 < K.brm2 ? K.k1 - inv : (a * inv) * u;
+    const float u = fmaf(-fabsf(t), K.iomb, 1.f);
+    umin = min_nan(umin, fabsf(u));
+    const float h = fmaf(a, fmaxf(u, 0.f), -1.f);
+    const float g = fmaf(h, inv, fminf(K.k1, inv));
     acc.x = fmaf(dx, g, acc.x);
     acc.y = fmaf(dy, g, acc.y);
     if (D == 3) acc.z = fmaf(dz, g, acc.z);
     return d2;
 }
+
+// True when the running minimum of |u| asks for the FP64 recomputation.
+__device__ __forceinline__ bool needs_fp64(const LoopK& K, float umin) { return !(umin >= K.uflag); }
 
 // Global sorted slot of staged candidate j (rare path and debug only).
 __device__ __forceinline__ int staged_global(const int* coff, const int* cglob, int ncell, int j) {
@@ -439,24 +486,22 @@ __device__ __forceinline__ int staged_global(const int* coff, const int* cglob, 
 // Staged candidates [ja, jb) of the target (a part of its neighbourhood
 // without the target itself), from a column-major staging (cand, with cell
 // offsets coff and global starts cglob of ncell cells).  Branch-free FP32:
-// every lane evaluates the Accelerator for every candidate.  A pair beyond
-// rmax needs no select: for d2 >= hi the triangle factor
-// u = 1 - |1 + beta - 2 d/rmax| / (1 - beta) is below -1e-6 even after FP32
-// rounding, so max(u, 0) = 0 and the term is an exact zero.  Pairs inside the
-// decision band (lo, hi) or below `tiny` (including other particles at the
-// same position) make the function return true: the caller then defers the
-// target to the FP64 fixup, which discards this partial sum.  SHIFT: some
-// candidates carry target-shift flags.
+// every lane evaluates the Accelerator for every candidate, and a pair
+// beyond rmax adds an exact zero (eval_candidate).  A candidate that needs
+// the FP64 decision (the |u| test of LoopK: the decision band around rmax,
+// coincident particles) makes the function return true: the caller then
+// defers the target to the FP64 fixup, which discards this partial sum.
+// SHIFT: some candidates carry target-shift flags.
 // SELF: the range holds the target itself at self_j; its copy is moved 8
-// units away (an exact zero term, no band or tiny flag), which sums to the
-// same bits as leaving it out, without a branch.
+// units away (an exact zero term, far from both zeros of u), which sums to
+// the same bits as leaving it out, without a branch.
 template <int D, bool DBG, bool SHIFT, bool SELF = false>
 __device__ __forceinline__ bool cand_range(const ForceArgs<D>& A, const ForceParams& P, const float4* cand,
                                            const int* coff, const int* cglob, const float* __restrict__ Mrow,
                                            int ncell, int ja, int jb, float px, float py, float pz, Acc& acc,
                                            int self_j = -1) {
     const float px1 = px - 1.f, py1 = py - 1.f, pz1 = pz - 1.f;
-    float bmin = INFINITY, dmin = INFINITY;
+    float umin = INFINITY;
     const LoopK K(P);
     for (int j = ja; j < jb; ++j) {
         float4 q = cand[j];
@@ -469,15 +514,15 @@ __device__ __forceinline__ bool cand_range(const ForceArgs<D>& A, const ForcePar
             if (D == 3) pze = (tb & kShiftZ) ? pz1 : pz;
             tb &= 0xffff;
         }
-        const float d2 = eval_candidate<D>(K, q.x, q.y, q.z, pxe, pye, pze, Mrow[tb], acc, bmin, dmin);
+        const float d2 = eval_candidate<D>(K, q.x, q.y, q.z, pxe, pye, pze, Mrow[tb], acc, umin);
         if (DBG && !(SELF && j == self_j)) {
             acc.cand++;
-            if ((d2 <= K.lo) & (d2 >= K.tiny))
+            if ((d2 <= K.lo) & (d2 > 0.f))
                 add_pair<D, true>(acc, make_float4(0.f, 0.f, 0.f, 0.f),
                                   id_of<D>(A, staged_global(coff, cglob, ncell, j)));
         }
     }
-    return (bmin < K.half) | (dmin < K.tiny);
+    return needs_fp64(K, umin);
 }
 
 // The target's neighbourhood read straight from global memory, for segments
@@ -494,7 +539,7 @@ __device__ __noinline__ bool direct_stencil(const ForceArgs<D>& A, const ForcePa
     const LoopK K(P);
     const int nx = P.g.nx;
     const bool wrap = P.wrap != 0;
-    float bmin = INFINITY, dmin = INFINITY;
+    float umin = INFINITY;
     for (int ci = 0; ci < 3; ++ci) {
         int col = cx - 1 + ci;
         bool qsx = false, tsx = false;
@@ -535,16 +580,16 @@ __device__ __noinline__ bool direct_stencil(const ForceArgs<D>& A, const ForcePa
                 if (qsy) q.y -= 1.f;
                 if (D == 3 && qsz) q.z -= 1.f;
                 const float d2 = eval_candidate<D>(K, q.x, q.y, q.z, pxe, pye, pze, Mrow[Layout<D>::type(q)], acc,
-                                                   bmin, dmin);
+                                                   umin);
                 if (DBG) {
                     acc.cand++;
-                    if ((d2 <= K.lo) & (d2 >= K.tiny))
+                    if ((d2 <= K.lo) & (d2 > 0.f))
                         add_pair<D, true>(acc, make_float4(0.f, 0.f, 0.f, 0.f), id_of<D>(A, j));
                 }
             }
         }
     }
-    return (bmin < K.half) | (dmin < K.tiny);
+    return needs_fp64(K, umin);
 }
 
 // Sum of `v` over the warp in a fixed butterfly order (the same bits on
