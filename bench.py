@@ -19,12 +19,15 @@ Our arm (default):
          events over a profiled pass of the same steps.
   cpu_baseline  the oracle (C FP64 restatement of the reference's step, all
          host threads) on a bounded sample of steps of the same workload.
+  cfg1_10k  the reference's default 10k world, 1,000 steps on the GPU and
+         through the oracle on all host threads.
   blobs_3d  the 4M-particle 3D blob world (uneven cells), device-resident.
   batched  512 uneven 2D worlds through plg_batch_* (autotuned) against the
          same worlds one at a time through single-world contexts.
-  serving  Poisson request arrivals through plg_server_* (scaled sizes, see
-         run_serving), completion latency p50/p99 and delivered throughput,
-         against a sample of the same requests run one at a time.
+  serving  the served configuration through plg_server_* (Poisson arrivals
+         over a bounded window, see run_serving): completed and unfinished
+         requests, completion latency p50/p99, delivered throughput and
+         device-busy fraction, against the same requests one at a time.
 --impl reference: the same workload through the oracle port on all host
 cores (the reference is Java and no JDK exists on either machine).
 
@@ -122,14 +125,20 @@ def parse(argv=None):
     ap.add_argument("--no-flush", action="store_true", help="keep L2 warm between steps (not a headline number)")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-worlds measurement")
     ap.add_argument("--batched-worlds", type=int, default=512)
-    ap.add_argument("--batched-steps", type=int, default=20)
+    ap.add_argument("--batched-steps", type=int, default=500, help="steps of the batched configuration")
+    ap.add_argument("--no-cfg1", action="store_true", help="skip the 10k-particle configuration")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving measurement")
     ap.add_argument("--no-3d", action="store_true", help="skip the 3D blob measurement")
     ap.add_argument("--steps-3d", type=int, default=20)
-    ap.add_argument("--serve-seconds", type=float, default=10.0)
+    ap.add_argument("--serve-seconds", type=float, default=60.0, help="arrival window of the serving run")
+    ap.add_argument("--serve-drain-s", type=float, default=60.0, help="longest drain after the arrival window")
     ap.add_argument("--serve-rate", type=float, default=200.0)
-    ap.add_argument("--serve-alone-s", type=float, default=3.0,
+    ap.add_argument("--serve-alone-s", type=float, default=10.0,
                     help="seconds of one-at-a-time stepping for the serving comparison")
+    ap.add_argument("--serve-cap-2d", type=float, default=48e6, help="2D batch capacity (particles)")
+    ap.add_argument("--serve-cap-3d", type=float, default=24e6, help="3D batch capacity (particles)")
+    ap.add_argument("--serve-cells-2d", type=float, default=24e6)
+    ap.add_argument("--serve-cells-3d", type=float, default=24e6)
     return ap.parse_args(argv)
 
 
@@ -207,6 +216,72 @@ def cpu_oracle_rate(n, threads, budget_s, steps_cap=None):
         steps = min(steps, steps_cap)
     t = w.run(steps, threads)
     return n * steps / t, steps, t
+
+
+CFG1 = dict(n=10_000, ntypes=6, steps=1000, seed=2023,
+            settings=dict(rmax=0.02, friction=FRICTION, force=1.0, dt=0.02, beta=0.3, wrap=True))
+
+
+def cfg1_world():
+    """The reference's own default world (Physics.setParticleCount(10000),
+    backend/Physics.java:79): 2D periodic, N = 10,000, 6 types uniform,
+    matrix uniform in [-1,1], positions uniform, velocities zero, rmax 0.02
+    (0.04 in [-1,1]^2), friction half-life 0.043 s, dt 0.02."""
+    rng = np.random.Generator(np.random.Philox(CFG1["seed"]))
+    n, t = CFG1["n"], CFG1["ntypes"]
+    pos = np.zeros((n, 3))
+    pos[:, :2] = rng.random((n, 2), dtype=np.float32)
+    types = rng.integers(0, t, n).astype(np.int32)
+    m = np.asarray(2 * rng.random((t, t)) - 1, np.float32).astype(np.float64)
+    return pos, np.zeros((n, 3)), types, m
+
+
+def cpu_cfg1(threads: int) -> dict:
+    """The 10k configuration's 1,000 steps through the oracle on `threads`
+    host threads (C FP64 restatement of Physics.update())."""
+    import orc
+
+    orc.build()
+    pos, vel, types, m = cfg1_world()
+    n = CFG1["n"]
+    S = CFG1["settings"]
+    w = orc.World(2, pos, vel, types, np.arange(n, dtype=np.int32), m,
+                  orc.settings(S["rmax"], S["friction"], S["force"], S["dt"], S["beta"], S["wrap"]))
+    w.run(5, threads)
+    t = w.run(CFG1["steps"], threads)
+    return {"value": n * CFG1["steps"] / t, "unit": UNIT, "ms_per_step": 1e3 * t / CFG1["steps"],
+            "steps": CFG1["steps"], "cores": threads, "kind": "port"}
+
+
+def run_cfg1(args) -> dict:
+    """The 10k configuration on the GPU: 1,000 steps enqueued at once
+    (plg_step_async), timed with CUDA events on the library's stream."""
+    import torch
+
+    from plgpu import _lib
+    from plgpu.physics import GpuWorld, check
+
+    pos, vel, types, m = cfg1_world()
+    n = CFG1["n"]
+    w = GpuWorld(2, n)
+    w.set_settings(**CFG1["settings"])
+    w.set_matrix(m)
+    w.upload(pos, vel, types)
+    w.step(args.warmup)
+    lib = _lib.load()
+    stream = torch.cuda.ExternalStream(w.stream())
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    a.record(stream)
+    check(lib.plg_step_async(w.ctx, CFG1["steps"]), w.ctx, "plg_step_async")
+    b.record(stream)
+    check(lib.plg_sync(w.ctx, 60.0), w.ctx, "plg_sync")
+    ms = a.elapsed_time(b)
+    w.close()
+    return {"metric": "particle-steps/s, 10k 2D (the reference's default world)", "value": n * CFG1["steps"] / (ms * 1e-3),
+            "unit": UNIT, "ms_per_step": ms / CFG1["steps"], "steps": CFG1["steps"],
+            "config": "2D periodic unit box, N=10,000, 6 types, rmax=0.02 (0.04 in [-1,1]^2), friction t1/2=0.043 s, "
+                      "dt=0.02, 1,000 steps (one CUDA graph launch per step); seeded Philox"}
 
 
 def run_batched(args) -> dict:
@@ -342,72 +417,109 @@ def plgpu_check(status, ctx, what):
 
 
 def run_serving(args) -> dict:
-    """The served configuration, bounded: Poisson arrivals at the configured
-    rate (200/s) for --serve-seconds, 50/50 2D/3D, types 3..16, k in [10, 50]
-    neighbours, 150 GB admission budget; N and steps are scaled down
-    (N log-uniform [1e3, 2e5] instead of [1e3, 2e6], steps U[100, 1000]
-    instead of [100, 5000]) so that the offered load stays near the device's
-    capacity and the run drains in about a minute."""
+    """The served configuration: Poisson arrivals at 200/s for an arrival
+    window of --serve-seconds (default 60 s), each request a world spec the
+    server generates on the device (2D or 3D 50/50, N log-uniform in
+    [1e3, 2e6], types 3..16, matrix uniform in [-1,1], k uniform in [10, 50]
+    neighbours, steps uniform in [100, 5000]), admitted under a 150 GB
+    device-memory budget and the batch capacities; then a drain of at most
+    --serve-drain-s.  The offered load (about 1.3e11 particle-steps/s) is far
+    above what one GPU delivers, so most requests are still queued when the
+    run ends: the line reports completed and unfinished requests, p50/p99
+    completion latency over the completed ones, the delivered rate, the
+    device-busy fraction of each batch, and the same requests one at a time
+    (each alone in a single-world context) for comparison."""
+    import threading
+
     from plgpu import workloads
+    from plgpu.physics import GpuWorld
     from plgpu.serve import Server
 
     rng = np.random.Generator(np.random.Philox(2025))
-    count = int(args.serve_rate * args.serve_seconds)
-    reqs = [workloads.serving_request(rng, n_lo=1_000, n_hi=200_000, steps_lo=100, steps_hi=1_000)
-            for _ in range(count)]
-    gaps = rng.exponential(1.0 / args.serve_rate, count)
-    offered = sum(w.pos.shape[0] * st for _, w, st in reqs) / args.serve_seconds
-    srv = Server(memory_budget_bytes=150 << 30, particle_capacity=(40_000_000, 40_000_000),
-                 cell_capacity=(60_000_000, 60_000_000), max_worlds_per_batch=1024, max_chunk_steps=16)
+    arrivals = []
+    t = 0.0
+    while True:
+        t += float(rng.exponential(1.0 / args.serve_rate))
+        if t > args.serve_seconds:
+            break
+        arrivals.append(t)
+    reqs = [workloads.serving_request_generated(rng) for _ in arrivals]
+    offered = sum(g.n * st for _, g, st in reqs) / args.serve_seconds
+    cap = (int(args.serve_cap_2d), int(args.serve_cap_3d))
+    cells = (int(args.serve_cells_2d), int(args.serve_cells_3d))
+    srv = Server(memory_budget_bytes=150 << 30, particle_capacity=cap, cell_capacity=cells,
+                 max_worlds_per_batch=1024, max_chunk_steps=16)
+    stop = threading.Event()
+
+    def collect():  # hands every finished result back to the host and drops it
+        while not stop.is_set():
+            rid = srv.wait_any(0.05)
+            if rid is not None:
+                srv.release(rid)
+
+    collector = threading.Thread(target=collect)
+    collector.start()
     t0 = time.perf_counter()
-    due = t0
-    ids = []
-    for (dim, w, st), gap in zip(reqs, gaps):
-        due += gap
-        delay = due - time.perf_counter()
+    for (dim, g, steps), ta in zip(reqs, arrivals):
+        delay = t0 + ta - time.perf_counter()
         if delay > 0:
             time.sleep(delay)
-        ids.append(srv.submit(dim, w, st))
-    for rid in ids:
-        srv.wait(rid, 600.0)
+        srv.submit_generated(dim, g, steps)
+    end = t0 + args.serve_seconds + args.serve_drain_s
+    while time.perf_counter() < end:
+        if srv.stats()["completed"] == len(reqs):
+            break
+        time.sleep(0.05)
     wall = time.perf_counter() - t0
     st = srv.stats()
-    for rid in ids:
-        srv.result(rid)
+    stop.set()
+    collector.join()
     srv.close()
-    # The same requests one at a time, each alone in a single-world context
-    # (plg_step of its whole step count; only the steps are timed), in
-    # arrival order until about --serve-alone-s seconds of stepping.
-    from plgpu.physics import GpuWorld
 
-    alone_ps, alone_s, alone_n = 0, 0.0, 0
-    for dim, w, steps in reqs:
-        g = GpuWorld(dim, w.pos.shape[0])
-        g.set_settings(w.rmax, w.friction, w.force, w.dt, beta=w.beta, wrap=w.wrap)
-        g.set_matrix(w.matrix)
-        g.upload(w.pos, w.vel, w.types)
+    # The same requests one at a time, each alone in a single-world context,
+    # in arrival order until --serve-alone-s seconds of stepping: a world's
+    # time per step does not depend on how many steps it runs, so each is
+    # timed over min(steps, 100) steps (after 2 untimed ones) and scaled to
+    # its step count.
+    alone_ps, alone_s, alone_n, measured = 0.0, 0.0, 0, 0.0
+    for dim, g, steps in reqs:
+        w = GpuWorld(dim, g.n)
+        w.set_settings(g.rmax, g.friction, g.force, g.dt, beta=g.beta, wrap=g.wrap)
+        w.set_matrix(g.matrix)
+        w.generate(g.n, g.position_setter, g.type_setter, g.seed)
+        w.step(2)
+        m = min(steps, 100)
         t1 = time.perf_counter()
-        g.step(steps)
-        alone_s += time.perf_counter() - t1
-        g.close()
-        alone_ps += w.pos.shape[0] * steps
+        w.step(m)
+        dt = time.perf_counter() - t1
+        w.close()
+        measured += dt
+        alone_s += dt * steps / m
+        alone_ps += g.n * steps
         alone_n += 1
-        if alone_s >= args.serve_alone_s:
+        if measured >= args.serve_alone_s:
             break
     alone = alone_ps / alone_s
     served = st["particle_steps"] / wall
     return {"metric": "served requests: completion latency and aggregate particle-steps/s",
-            "requests": count, "completed": st["completed"], "latency_p50_ms": st["latency_p50_ms"],
-            "latency_p99_ms": st["latency_p99_ms"], "latency_mean_ms": st["latency_mean_ms"],
+            "requests": len(reqs), "completed": st["completed"],
+            "unfinished": {"queued": st["queued"], "resident": st["running"]},
+            "latency_p50_ms": st["latency_p50_ms"], "latency_p99_ms": st["latency_p99_ms"],
+            "latency_mean_ms": st["latency_mean_ms"],
             "value": served, "unit": UNIT, "offered_particle_steps_per_s": offered,
+            "device_busy_fraction": {"2d": st["busy_dim_s"][0] / wall, "3d": st["busy_dim_s"][1] / wall},
+            "compactions": st["compactions"],
             "one_at_a_time": {"value": alone, "unit": UNIT, "requests": alone_n,
-                              "how": "the first requests in arrival order, each in its own context, plg_step of its "
-                                     "step count, steps timed alone (host wall clock)"},
+                              "how": "the first requests in arrival order, each generated alone in a single-world "
+                                     "context, min(steps, 100) steps timed (host wall clock) and scaled to its step "
+                                     "count"},
             "speedup_vs_one_at_a_time": served / alone,
-            "wall_s": wall, "peak_resident_bytes": st["peak_resident_bytes"],
-            "config": f"Poisson arrivals {args.serve_rate:g}/s for {args.serve_seconds:g} s, 2D/3D 50/50, "
-                      "N log-uniform [1e3, 2e5], types 3..16, k U[10, 50], steps U[100, 1000], budget 150 GB, "
-                      "chunks of <= 16 steps; seeded Philox"}
+            "wall_s": wall, "peak_resident_bytes": st["peak_resident_bytes"], "budget_bytes": 150 << 30,
+            "config": f"Poisson arrivals {args.serve_rate:g}/s for {args.serve_seconds:g} s (then at most "
+                      f"{args.serve_drain_s:g} s of drain), 2D/3D 50/50, N log-uniform [1e3, 2e6], types 3..16, "
+                      "k U[10, 50], steps U[100, 5000], worlds generated on the device (uniform positions and "
+                      f"types, seeded), budget 150 GB, batch capacities {cap[0]:,} (2D) / {cap[1]:,} (3D) "
+                      "particles, chunks of <= 16 steps; seeded Philox"}
 
 
 def run_reference(args):
@@ -436,6 +548,7 @@ def run_reference(args):
                          "sample": f"{args.steps} full steps after {args.warmup} warm-up steps (Java/JDK absent: "
                                    "C restatement of the reference's step, same algorithm and threading)"},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "cfg1_10k": cpu_cfg1(threads),
     }
     print(json.dumps(line))
 
@@ -607,6 +720,12 @@ def run_ours(args):
             gbs = b / (kern[name]["avg_us"] * 1e-6) / 1e9
             sort_kernels[name] = {"achieved_gbs": gbs, "frac_of_measured_hbm": gbs / hbm}
 
+    cfg1 = None
+    if rank == 0 and not args.no_cfg1:
+        cfg1 = run_cfg1(args)
+        if not args.no_cpu_baseline:
+            cfg1["cpu_baseline"] = cpu_cfg1(os.cpu_count() or 1)
+            cfg1["speedup_vs_cpu"] = cfg1["value"] / cfg1["cpu_baseline"]["value"]
     blobs3d = None
     if rank == 0 and not args.no_3d:
         blobs3d = run_blobs_3d(args)
@@ -653,6 +772,7 @@ def run_ours(args):
             "candidates_per_particle": cand,
             "interactions_per_particle": inter,
             "cpu_baseline": cpu,
+            "cfg1_10k": cfg1,
             "blobs_3d": blobs3d,
             "batched": batched,
             "serving": serving,

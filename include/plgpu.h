@@ -446,9 +446,13 @@ int plg_batch_debug_step(plg_batch* batch, int32_t* cell, int32_t* pairs,
  * packs every active world into one batch per dimension (the 2D and 3D
  * batches run concurrently on their own streams), advances them in chunks
  * of at most max_chunk_steps steps (never past a world's own count) and
- * hands back each final state.  Requests that arrive while others run join
- * at the next chunk boundary.  Each result is bit for bit the world run
- * alone. */
+ * hands back each final state.  Membership changes overlap the steps: an
+ * admitted world is converted (or generated) into the batch's free tail on
+ * a side stream while a chunk runs and joins at the next chunk boundary; a
+ * finished world stays frozen in place and is downloaded on the side stream
+ * while the next chunk runs; retired worlds are compacted away in one pass
+ * only when they take a quarter of the batch or block an admission.  Each
+ * result is bit for bit the world run alone. */
 typedef struct plg_server plg_server;
 
 typedef struct plg_server_config {
@@ -468,16 +472,37 @@ typedef struct plg_server_stats_t {
     int64_t submitted, completed, queued, running;
     int64_t resident_bytes, peak_resident_bytes;
     double particle_steps;   /* advanced so far, all worlds */
-    double busy_s, wall_s;   /* time the scheduler spent in chunks / since create */
+    double busy_s, wall_s;   /* device time of the step chunks (both batches) / time since create */
     double latency_p50_ms, latency_p99_ms, latency_mean_ms;  /* submit -> result on host */
+    double busy_dim_s[2];    /* device time of the step chunks of the 2D and of the 3D batch */
+    int64_t compactions;     /* re-layout passes that dropped finished worlds */
 } plg_server_stats_t;
 
 int plg_server_create(const plg_server_config* cfg, plg_server** out);
 /* Copies the world; PLG_E_CAPACITY for a request that could never fit. */
 int plg_server_submit(plg_server* server, int32_t dim, const plg_world_desc* world, int32_t steps,
                       int64_t* request_id);
+
+/* A world given by its generator instead of its particles: n particles made
+ * on the device at admission exactly as plg_generate makes them in a
+ * single-world context (Physics.setParticleCount from nothing with catalogue
+ * setters, Physics.java:190-196, 285-295), so a request carries a few bytes
+ * however large its world.  `world.pos`, `world.vel` and `world.type` are
+ * ignored. */
+typedef struct plg_world_gen {
+    plg_world_desc world;     /* settings, ntypes, matrix, n */
+    int32_t position_setter;  /* PLG_POS_* */
+    int32_t type_setter;      /* PLG_TYPE_* */
+    uint64_t seed;
+} plg_world_gen;
+int plg_server_submit_generated(plg_server* server, int32_t dim, const plg_world_gen* world, int32_t steps,
+                                int64_t* request_id);
 /* Waits for a request (timeout_s <= 0: no limit); *state = PLG_REQ_*. */
 int plg_server_wait(plg_server* server, int64_t request_id, double timeout_s, int32_t* state);
+/* Waits for any request to finish (timeout_s <= 0: no limit) and gives its
+ * id; every finished request is given once, in completion order.
+ * PLG_E_TIMEOUT when none finished in time. */
+int plg_server_wait_any(plg_server* server, double timeout_s, int64_t* request_id);
 /* Copies a finished request's final state (cell-sorted order, like
  * plg_download) and releases it; any pointer may be NULL. */
 int plg_server_result(plg_server* server, int64_t request_id, double* pos, double* vel, int32_t* type,

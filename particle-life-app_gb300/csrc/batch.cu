@@ -43,6 +43,7 @@ struct WorldRec {
     std::vector<float> matrix;  // ntypes^2
     int64_t p_off = 0, c_off = 0, m_off = 0, b_off = 0;
     int32_t steps_left = INT32_MAX;  // steps before the world freezes (INT32_MAX: no limit)
+    bool dead = false;               // retired: frozen in place until the next compaction
 };
 
 }  // namespace
@@ -91,6 +92,16 @@ struct plg_batch {
     int32_t* dbg_cell = nullptr;
 
     std::vector<WorldRec> worlds;  // device order
+    // Incremental membership (the serving loop): worlds converted into the
+    // free tail [n_total, ...) of the arrays while steps run, joining at
+    // batch_commit; retired worlds stay frozen in place until batch_compact.
+    std::vector<WorldRec> pending;
+    int64_t pend_n = 0, pend_c = 0;  // tail particles and cells of the pending worlds
+    int64_t tab_b = 0, tab_m = 0;    // next free entry of the bounds and matrix tables
+    int64_t dead_n = 0;              // particles of retired worlds still in the layout
+    bool pageable = false;           // the device reads and writes pageable host memory
+    unsigned char* side_stage = nullptr;  // staging of tail conversions and downloads
+    int64_t side_stage_cap = 0;
     int32_t next_id = 1;
     int variant = 0;  // force kernel tile variant (autotuner)
     int64_t n_total = 0, c_total = 0;
@@ -184,7 +195,7 @@ void free_batch(plg_batch* b) {
                     b->status_d, b->worlds_d,  b->wp_off_d,  b->move_new_d,  b->move_old_d, b->bounds_d,
                     b->tile_off_d, b->steps_left_d,
                     b->matrix_d, b->stage,     b->dbg_pairs, b->dbg_hsum,    b->dbg_hxor, b->dbg_cand,
-                    b->dbg_acc,  b->dbg_cell};
+                    b->dbg_acc,  b->dbg_cell,  b->side_stage};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (b->status_h) cudaFreeHost(b->status_h);
@@ -221,6 +232,25 @@ int check_world(int dim, const plg_world_desc& d, std::string* msg) {
             if (d.vel && !std::isfinite(d.vel[3 * i + k])) return fail(PLG_E_INVALID_ARG, "velocities must be finite");
         }
         if (d.type[i] < 0 || d.type[i] >= d.ntypes) return fail(PLG_E_INVALID_ARG, "types must lie in [0, matrix size)");
+    }
+    return PLG_OK;
+}
+
+// The checks of a world generated on the device (no particle arrays).
+int check_generated(int dim, const plg_world_desc& d, std::string* msg) {
+    plg_world_desc e = d;
+    e.n = 0;
+    e.pos = e.vel = nullptr;
+    e.type = nullptr;
+    const int rc = check_world(dim, e, msg);
+    if (rc) return rc;
+    if (d.n < 0) {
+        if (msg) *msg = "negative particle count";
+        return PLG_E_INVALID_ARG;
+    }
+    if (d.n > kMaxParticles) {
+        if (msg) *msg = "too many particles";
+        return PLG_E_CAPACITY;
     }
     return PLG_OK;
 }
@@ -351,6 +381,11 @@ int relayout(plg_batch* b, const std::vector<int>& survivors, const plg_world_de
     b->worlds = std::move(next);
     b->n_total = p;
     b->c_total = c;
+    b->tab_b = bo;
+    b->tab_m = m;
+    b->dead_n = 0;
+    for (const WorldRec& w : b->worlds)
+        if (w.dead) b->dead_n += w.n;
     if ((rc = upload_tables(b))) return rc;  // synchronises: the move tables above are consumed
     BCK(b, cudaMemsetAsync(b->counts, 0, sizeof(uint32_t) * (size_t)std::max<int64_t>(c, 1), st));
     BCK(b, cudaMemsetAsync(b->status_d, 0, sizeof(uint32_t), st));
@@ -480,6 +515,260 @@ int wait_batch(plg_batch* b, double timeout_s) {
 
 }  // namespace
 
+// ---- incremental membership, for the serving loop ----------------------
+//
+// A batch keeps its worlds at the front of its arrays; the rest is a free
+// tail.  batch_append converts (or generates) a new world straight into the
+// tail on a side stream while steps run on the batch stream: a step touches
+// only slots below n_total and cells below c_total, so the two never meet.
+// batch_commit then makes the tail worlds part of the step (tables, graph).
+// A finished world is retired in place: its step budget is spent, so the
+// step leaves it frozen (its state and order untouched) and it can be
+// downloaded on the side stream while later steps run; batch_compact drops
+// retired worlds with one re-layout pass once they take too much room.
+
+namespace plg {
+
+namespace {
+
+template <int D>
+int append_world(plg_batch* b, const plg_world_desc& d, const WorldGen* gen, int32_t steps, cudaStream_t side,
+                 int32_t* id_out) {
+    WorldRec w;
+    w.n = d.n;
+    w.ntypes = d.ntypes;
+    w.s = d.settings;
+    w.nx = grid_n(d.settings.rmax);
+    w.ncells = (int64_t)w.nx * w.nx * (D == 3 ? w.nx : 1);
+    const int64_t nbounds = w.nx + 1, nmat = (int64_t)d.ntypes * d.ntypes;
+    if (b->n_total + b->pend_n + w.n > b->pcap) return berr(b, PLG_E_CAPACITY, "batch particle capacity exceeded");
+    if (b->c_total + b->pend_c + w.ncells > b->ccap) return berr(b, PLG_E_CAPACITY, "batch cell capacity exceeded");
+    if ((int64_t)(b->worlds.size() + b->pending.size()) + 1 > b->wcap)
+        return berr(b, PLG_E_CAPACITY, "batch world capacity exceeded");
+    if (b->tab_b + nbounds > b->bounds_cap || b->tab_m + nmat > b->matrix_cap)
+        return berr(b, PLG_E_CAPACITY, "batch tables full (batch_reserve_tables)");
+    w.id = b->next_id++;
+    w.steps_left = steps < 0 ? INT32_MAX : steps;
+    w.bounds.resize((size_t)nbounds);
+    build_bounds(d.settings.rmax, w.nx, w.bounds.data());
+    w.matrix.resize((size_t)nmat);
+    for (size_t q = 0; q < w.matrix.size(); ++q) w.matrix[q] = (float)d.matrix[q];
+    w.p_off = b->n_total + b->pend_n;
+    w.c_off = b->c_total + b->pend_c;
+    w.b_off = b->tab_b;
+    w.m_off = b->tab_m;
+    // The tail's cells may hold counts of a world a compaction dropped.
+    BCK(b, cudaMemsetAsync(b->counts + w.c_off, 0, sizeof(uint32_t) * (size_t)w.ncells, side));
+    // Pageable source: copied out before cudaMemcpyAsync returns.
+    BCK(b, cudaMemcpyAsync(b->bounds_d + w.b_off, w.bounds.data(), sizeof(float) * nbounds, cudaMemcpyHostToDevice,
+                           side));
+    Grid g{};
+    g.nx = w.nx;
+    g.ncells = (int)w.ncells;
+    g.inv_cs = (float)(1.0 / w.s.rmax);
+    g.b_nx = w.bounds[w.nx];
+    g.bounds = b->bounds_d + w.b_off;
+    if (w.n > 0 && gen) {
+        launch_generate<D>(side, (int)w.n, gen->position_setter, gen->type_setter, gen->seed, w.ntypes,
+                           w.s.wrap ? 1 : 0, sbuf<D>(b->apt, b->avel, w.p_off));
+        launch_rebin<D>(side, (int)w.n, sbuf<D>(b->apt, b->avel, w.p_off), b->cell + w.p_off, b->counts, g,
+                        (uint32_t)w.c_off);
+        BCK(b, cudaGetLastError());
+    } else if (w.n > 0) {
+        // Page-locked arrays are read in place; so is pageable memory on a
+        // device that reads it coherently; anything else is staged.
+        const double* dpos = mapped_host(d.pos);
+        const double* dvel = mapped_host(d.vel);
+        const int32_t* dtype = mapped_host(d.type);
+        if (b->pageable) {
+            if (!dpos) dpos = d.pos;
+            if (!dvel) dvel = d.vel;
+            if (!dtype) dtype = d.type;
+        }
+        if (!dpos || (d.vel && !dvel) || !dtype) {
+            const int64_t rows = (w.n + 1) & ~(int64_t)1;
+            const int64_t need = (int64_t)batch_stage_bytes(rows);
+            if (need > b->side_stage_cap) {
+                BCK(b, cudaStreamSynchronize(side));
+                if (b->side_stage) cudaFree(b->side_stage);
+                b->side_stage = nullptr;
+                b->side_stage_cap = 0;
+                if (cudaMalloc((void**)&b->side_stage, (size_t)need) != cudaSuccess) {
+                    cudaGetLastError();
+                    return berr(b, PLG_E_NO_MEMORY, "cudaMalloc (side staging)");
+                }
+                b->side_stage_cap = need;
+            }
+            double* spos = (double*)b->side_stage;
+            double* svel = spos + 3 * rows;
+            int32_t* stype = (int32_t*)(svel + 3 * rows);
+            if (!dpos) {
+                BCK(b, cudaMemcpyAsync(spos, d.pos, sizeof(double) * 3 * w.n, cudaMemcpyHostToDevice, side));
+                dpos = spos;
+            }
+            if (d.vel && !dvel) {
+                BCK(b, cudaMemcpyAsync(svel, d.vel, sizeof(double) * 3 * w.n, cudaMemcpyHostToDevice, side));
+                dvel = svel;
+            }
+            if (!dtype) {
+                BCK(b, cudaMemcpyAsync(stype, d.type, sizeof(int32_t) * w.n, cudaMemcpyHostToDevice, side));
+                dtype = stype;
+            }
+        }
+        launch_upload<D>(side, (int)w.n, dpos, dvel, dtype, w.ntypes, sbuf<D>(b->apt, b->avel, w.p_off),
+                         b->cell + w.p_off, b->counts, g, b->status_d, (uint32_t)w.c_off);
+        BCK(b, cudaGetLastError());
+    }
+    b->pend_n += w.n;
+    b->pend_c += w.ncells;
+    b->tab_b += nbounds;
+    b->tab_m += nmat;
+    if (id_out) *id_out = w.id;
+    b->pending.push_back(std::move(w));
+    return PLG_OK;
+}
+
+}  // namespace
+
+int batch_append(plg_batch* b, const plg_world_desc& d, const WorldGen* gen, int32_t steps, cudaStream_t side,
+                 int32_t* id_out) {
+    if (!b) return PLG_E_INVALID_ARG;
+    std::string msg;
+    const int rc = gen ? check_generated(b->dim, d, &msg) : check_world(b->dim, d, &msg);
+    if (rc) return berr(b, rc, msg);
+    if (gen && (gen->position_setter < 0 || gen->position_setter >= kPosCount || gen->type_setter < 0 ||
+                gen->type_setter >= kTypeCount))
+        return berr(b, PLG_E_INVALID_ARG, "unknown setter");
+    BatchDeviceGuard g(b->device);
+    return b->dim == 2 ? append_world<2>(b, d, gen, steps, side, id_out) : append_world<3>(b, d, gen, steps, side, id_out);
+}
+
+bool batch_fits(const plg_batch* b, int64_t n, int64_t cells, bool after_compaction) {
+    int64_t live_n = b->n_total + b->pend_n, live_c = b->c_total + b->pend_c;
+    int64_t live_w = (int64_t)(b->worlds.size() + b->pending.size());
+    if (after_compaction)
+        for (const WorldRec& w : b->worlds)
+            if (w.dead) {
+                live_n -= w.n;
+                live_c -= w.ncells;
+                live_w -= 1;
+            }
+    return live_n + n <= b->pcap && live_c + cells <= b->ccap && live_w + 1 <= b->wcap;
+}
+
+int batch_reserve_tables(plg_batch* b, int64_t bounds_floats, int64_t matrix_floats) {
+    if (!b) return PLG_E_INVALID_ARG;
+    BatchDeviceGuard g(b->device);
+    const int64_t nb = b->tab_b + bounds_floats, nm = b->tab_m + matrix_floats;
+    if (nb <= b->bounds_cap && nm <= b->matrix_cap) return PLG_OK;
+    if (!b->pending.empty()) return berr(b, PLG_E_STATE, "tables grow only without pending worlds");
+    // The tables move: regrow waits for the batch stream, and the caller's
+    // side stream has no tail work (nothing is pending).
+    int rc;
+    if ((rc = regrow(b, &b->bounds_d, &b->bounds_cap, std::max(nb, 2 * b->bounds_cap), "bounds"))) return rc;
+    if ((rc = regrow(b, &b->matrix_d, &b->matrix_cap, std::max(nm, 2 * b->matrix_cap), "matrix"))) return rc;
+    return upload_tables(b);  // the committed worlds' tables, at their offsets
+}
+
+int batch_commit(plg_batch* b) {
+    if (!b) return PLG_E_INVALID_ARG;
+    if (b->pending.empty()) return PLG_OK;
+    BatchDeviceGuard g(b->device);
+    for (WorldRec& w : b->pending) {
+        b->n_total += w.n;
+        b->c_total += w.ncells;
+        b->worlds.push_back(std::move(w));
+    }
+    b->pending.clear();
+    b->pend_n = b->pend_c = 0;
+    destroy_batch_graph(b);
+    int rc = upload_tables(b);  // synchronises the batch stream
+    if (rc) return rc;
+    BCK(b, cudaMemcpy(b->status_h, b->status_d, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    if (*b->status_h & (kDevBadPosition | kDevBadType | kDevBadVelocity))
+        return berr(b, PLG_E_DEVICE, "a conversion kernel flagged invalid input");
+    return PLG_OK;
+}
+
+int batch_retire(plg_batch* b, int32_t id) {
+    if (!b) return PLG_E_INVALID_ARG;
+    const int k = find_world(b, id);
+    if (k < 0) return berr(b, PLG_E_INVALID_ARG, "unknown world id " + std::to_string(id));
+    WorldRec& w = b->worlds[(size_t)k];
+    if (w.dead) return PLG_OK;
+    if (w.steps_left != 0) return berr(b, PLG_E_STATE, "only a frozen world (no steps left) can be retired");
+    w.dead = true;
+    b->dead_n += w.n;
+    return PLG_OK;
+}
+
+int64_t batch_dead_particles(const plg_batch* b) { return b ? b->dead_n : 0; }
+
+int batch_download_on(plg_batch* b, int32_t id, cudaStream_t st, double* pos, double* vel, int32_t* type,
+                      int32_t* pid) {
+    if (!b) return PLG_E_INVALID_ARG;
+    const int k = find_world(b, id);
+    if (k < 0) return berr(b, PLG_E_INVALID_ARG, "unknown world id " + std::to_string(id));
+    const WorldRec& w = b->worlds[(size_t)k];
+    if (w.n == 0) return PLG_OK;
+    BatchDeviceGuard g(b->device);
+    double *kpos = mapped_host(pos), *kvel = mapped_host(vel);
+    int32_t *ktype = mapped_host(type), *kid = mapped_host(pid);
+    if (b->pageable) {
+        if (!kpos) kpos = pos;
+        if (!kvel) kvel = vel;
+        if (!ktype) ktype = type;
+        if (!kid) kid = pid;
+    }
+    const bool staged = (pos && !kpos) || (vel && !kvel) || (type && !ktype) || (pid && !kid);
+    const int64_t rows = (w.n + 1) & ~(int64_t)1;
+    if (staged && (int64_t)batch_stage_bytes(rows) > b->side_stage_cap) {
+        BCK(b, cudaStreamSynchronize(st));
+        if (b->side_stage) cudaFree(b->side_stage);
+        b->side_stage = nullptr;
+        b->side_stage_cap = 0;
+        if (cudaMalloc((void**)&b->side_stage, batch_stage_bytes(rows)) != cudaSuccess) {
+            cudaGetLastError();
+            return berr(b, PLG_E_NO_MEMORY, "cudaMalloc (side staging)");
+        }
+        b->side_stage_cap = (int64_t)batch_stage_bytes(rows);
+    }
+    double* spos = (double*)b->side_stage;
+    double* svel = spos + 3 * rows;
+    int32_t* stype = (int32_t*)(svel + 3 * rows);
+    int32_t* sid = stype + rows;
+    if (pos && !kpos) kpos = spos;
+    if (vel && !kvel) kvel = svel;
+    if (type && !ktype) ktype = stype;
+    if (pid && !kid) kid = sid;
+    if (b->dim == 2)
+        launch_download<2>(st, (int)w.n, sbuf<2>(b->apt, b->avel, w.p_off), kpos, kvel, ktype, kid);
+    else
+        launch_download<3>(st, (int)w.n, sbuf<3>(b->apt, b->avel, w.p_off), kpos, kvel, ktype, kid);
+    BCK(b, cudaGetLastError());
+    const size_t n = (size_t)w.n;
+    if (pos && kpos == spos) BCK(b, cudaMemcpyAsync(pos, spos, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, st));
+    if (vel && kvel == svel) BCK(b, cudaMemcpyAsync(vel, svel, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, st));
+    if (type && ktype == stype)
+        BCK(b, cudaMemcpyAsync(type, stype, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, st));
+    if (pid && kid == sid) BCK(b, cudaMemcpyAsync(pid, sid, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, st));
+    return PLG_OK;
+}
+
+int batch_compact(plg_batch* b) {
+    if (!b) return PLG_E_INVALID_ARG;
+    if (!b->pending.empty()) return berr(b, PLG_E_STATE, "commit pending worlds before a compaction");
+    if (b->dead_n == 0) return PLG_OK;
+    std::vector<int> survivors;
+    for (size_t k = 0; k < b->worlds.size(); ++k)
+        if (!b->worlds[k].dead) survivors.push_back((int)k);
+    BatchDeviceGuard g(b->device);
+    return b->dim == 2 ? relayout<2>(b, survivors, nullptr, 0, nullptr)
+                       : relayout<3>(b, survivors, nullptr, 0, nullptr);
+}
+
+}  // namespace plg
+
 extern "C" {
 
 int plg_world_check(int32_t dim, const plg_world_desc* d) {
@@ -509,11 +798,14 @@ int plg_batch_create(int32_t dim, int64_t particle_capacity, int32_t world_capac
     b->pcap = particle_capacity;
     b->wcap = world_capacity;
     b->ccap = cell_capacity;
-    if (cudaGetDevice(&b->device) != cudaSuccess) {
+    int pageable = 0;
+    if (cudaGetDevice(&b->device) != cudaSuccess ||
+        cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, b->device) != cudaSuccess) {
         cudaGetLastError();
         delete b;
         return PLG_E_CUDA;
     }
+    b->pageable = pageable != 0;
     int rc = PLG_OK;
     auto dm = [&](void** p, size_t bytes) {
         if (rc) return;
@@ -572,6 +864,7 @@ int plg_batch_update(plg_batch* b, int32_t nremove, const int32_t* remove_ids, i
     if (!b) return PLG_E_INVALID_ARG;
     if (nremove < 0 || nadd < 0) return berr(b, PLG_E_INVALID_ARG, "negative world count");
     if ((nremove > 0 && !remove_ids) || (nadd > 0 && !add)) return berr(b, PLG_E_INVALID_ARG, "NULL world list");
+    if (!b->pending.empty()) return berr(b, PLG_E_STATE, "worlds appended to the tail are not committed yet");
     std::vector<char> gone(b->worlds.size(), 0);
     for (int32_t r = 0; r < nremove; ++r) {
         const int k = find_world(b, remove_ids[r]);

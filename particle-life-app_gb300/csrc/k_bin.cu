@@ -160,16 +160,17 @@ __global__ void k_batch_tick(int* steps_left, int nworlds) {
     if (k < nworlds && steps_left[k] > 0) steps_left[k] -= 1;
 }
 
-// Re-binning of the current state (after an rmax change).
+// Re-binning of the current state (after an rmax change, or of a world
+// generated on the device; cell_base: the world's first global cell).
 template <int D>
 __global__ void __launch_bounds__(kThreads) k_rebin(int n, StateBuf<D> a, uint32_t* __restrict__ cell,
-                                                    uint32_t* counts, Grid g) {
+                                                    uint32_t* counts, Grid g, uint32_t cell_base) {
     const int i = blockIdx.x * kThreads + threadIdx.x;
     const bool valid = i < n;
     uint32_t c = 0;
     if (valid) {
         const float4 p = a.pt[i];
-        c = cell_index<D>(p.x, p.y, D == 3 ? p.z : 0.f, g);
+        c = cell_base + cell_index<D>(p.x, p.y, D == 3 ? p.z : 0.f, g);
     }
     const unsigned mask = __ballot_sync(kFull, valid);
     if (valid) {
@@ -459,9 +460,10 @@ template void launch_batch_rebin<3>(cudaStream_t, int, StateBuf<3>, const ForceP
                                     uint32_t*);
 
 template <int D>
-void launch_rebin(cudaStream_t st, int n, StateBuf<D> a, uint32_t* cell, uint32_t* counts, Grid g) {
+void launch_rebin(cudaStream_t st, int n, StateBuf<D> a, uint32_t* cell, uint32_t* counts, Grid g,
+                  uint32_t cell_base) {
     if (n <= 0) return;
-    k_rebin<D><<<blocks_for(n, kThreads), kThreads, 0, st>>>(n, a, cell, counts, g);
+    k_rebin<D><<<blocks_for(n, kThreads), kThreads, 0, st>>>(n, a, cell, counts, g, cell_base);
 }
 
 template <int D>
@@ -495,8 +497,8 @@ template void launch_upload<2>(cudaStream_t, int, const double*, const double*, 
                                uint32_t*, uint32_t*, Grid, uint32_t*, uint32_t, int);
 template void launch_upload<3>(cudaStream_t, int, const double*, const double*, const int32_t*, int, StateBuf<3>,
                                uint32_t*, uint32_t*, Grid, uint32_t*, uint32_t, int);
-template void launch_rebin<2>(cudaStream_t, int, StateBuf<2>, uint32_t*, uint32_t*, Grid);
-template void launch_rebin<3>(cudaStream_t, int, StateBuf<3>, uint32_t*, uint32_t*, Grid);
+template void launch_rebin<2>(cudaStream_t, int, StateBuf<2>, uint32_t*, uint32_t*, Grid, uint32_t);
+template void launch_rebin<3>(cudaStream_t, int, StateBuf<3>, uint32_t*, uint32_t*, Grid, uint32_t);
 template void launch_download<2>(cudaStream_t, int, StateBuf<2>, double*, double*, int32_t*, int32_t*);
 template void launch_download<3>(cudaStream_t, int, StateBuf<3>, double*, double*, int32_t*, int32_t*);
 template void launch_gather<2>(cudaStream_t, int, const uint32_t*, const uint32_t*, const uint32_t*, StateBuf<2>,

@@ -160,6 +160,9 @@ struct ForceParams {
     float m2_inv_rmax;      // -2 / rmax
     float beta_rmax;        // beta * rmax: below this distance the linear repulsion applies
     float k1;               // 1 / (beta * rmax): (|d|/(beta rmax) - 1) / |d| = k1 - 1/|d|
+    float att_k;            // 2 / ((1 - beta) rmax): the triangle's slope per unit distance
+    float att_a0;           // -2 beta / (1 - beta): A = |d| att_k + att_a0 = (s - beta) 2/(1 - beta)
+    float att_b0;           // 2 / (1 - beta):       B = att_b0 - |d| att_k = (1 - s) 2/(1 - beta)
     float ff;               // (float) pow(friction, 60 dt)
     float scale;            // (float) (rmax * force * dt)
     float dt;
@@ -283,7 +286,8 @@ void launch_batch_rebin(cudaStream_t st, int n, StateBuf<D> a, const ForceParams
                         uint32_t* cell, uint32_t* counts);
 
 template <int D>
-void launch_rebin(cudaStream_t st, int n, StateBuf<D> a, uint32_t* cell, uint32_t* counts, Grid g);
+void launch_rebin(cudaStream_t st, int n, StateBuf<D> a, uint32_t* cell, uint32_t* counts, Grid g,
+                  uint32_t cell_base = 0);
 
 template <int D>
 void launch_download(cudaStream_t st, int n, StateBuf<D> a, double* pos, double* vel, int32_t* type,

@@ -66,6 +66,9 @@ void fill_force_params(const plg_settings& s, int nx, int64_t ncells, int ntypes
     p.m2_inv_rmax = (float)(-2.0 / s.rmax);
     p.beta_rmax = (float)(s.beta * s.rmax);
     p.k1 = (float)(1.0 / (s.beta * s.rmax));
+    p.att_k = (float)(2.0 / ((1.0 - s.beta) * s.rmax));
+    p.att_a0 = (float)(-2.0 * s.beta / (1.0 - s.beta));
+    p.att_b0 = (float)(2.0 / (1.0 - s.beta));
     p.ff = (float)std::pow(s.friction, 60 * s.dt);
     p.scale = (float)(s.rmax * s.force * s.dt);
     p.dt = (float)s.dt;

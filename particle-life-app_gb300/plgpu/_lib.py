@@ -102,7 +102,14 @@ class plg_server_stats_t(C.Structure):
         ("latency_p50_ms", C.c_double),
         ("latency_p99_ms", C.c_double),
         ("latency_mean_ms", C.c_double),
+        ("busy_dim_s", C.c_double * 2),
+        ("compactions", C.c_int64),
     ]
+
+
+class plg_world_gen(C.Structure):
+    _fields_ = [("world", plg_world_desc), ("position_setter", C.c_int32), ("type_setter", C.c_int32),
+                ("seed", C.c_uint64)]
 
 
 PLG_REQ_QUEUED = 0
@@ -193,7 +200,9 @@ SIGNATURES = {
     "plg_world_device_bytes": (C.c_int64, [C.c_int32, C.POINTER(plg_world_desc)]),
     "plg_server_create": (C.c_int, [C.POINTER(plg_server_config), C.POINTER(_P)]),
     "plg_server_submit": (C.c_int, [_P, C.c_int32, C.POINTER(plg_world_desc), C.c_int32, _I64P]),
+    "plg_server_submit_generated": (C.c_int, [_P, C.c_int32, C.POINTER(plg_world_gen), C.c_int32, _I64P]),
     "plg_server_wait": (C.c_int, [_P, C.c_int64, C.c_double, _I32P]),
+    "plg_server_wait_any": (C.c_int, [_P, C.c_double, _I64P]),
     "plg_server_result": (C.c_int, [_P, C.c_int64, _DP, _DP, _I32P, _I32P, _I64P, _DP]),
     "plg_server_stats": (C.c_int, [_P, C.POINTER(plg_server_stats_t)]),
     "plg_server_last_error": (C.c_char_p, [_P]),

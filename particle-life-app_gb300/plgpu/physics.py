@@ -219,11 +219,15 @@ def check(status: int, ctx=None, what: str = "") -> None:
 
 def _resident(shape, dtype) -> np.ndarray:
     """An uninitialised array whose pages the CPU has written once (one byte
-    per 4 KB), so that they are resident before the device writes the array
-    in place; far cheaper than filling it."""
+    per page, and the last byte: the array rarely starts on a page
+    boundary, so its last page may begin less than a page before its end),
+    so that they are resident before the device writes the array in place;
+    far cheaper than filling it."""
     a = np.empty(shape, dtype)
     if a.size:
-        a.reshape(-1).view(np.uint8)[::4096] = 0
+        b = a.reshape(-1).view(np.uint8)
+        b[::4096] = 0
+        b[-1] = 0
     return a
 
 

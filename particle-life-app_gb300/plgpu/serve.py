@@ -7,12 +7,46 @@ is collected.
 """
 from __future__ import annotations
 
+from dataclasses import dataclass
 from typing import Optional
 
 import numpy as np
 
 from . import _lib
 from .batch import WorldDesc, world_struct
+
+
+@dataclass
+class GeneratedWorld:
+    """A world given by its generator (plg_world_gen): n particles made on the
+    device at admission, exactly as GpuWorld.generate makes them."""
+
+    n: int
+    matrix: np.ndarray  # (t, t) float64
+    rmax: float
+    friction: float
+    force: float = 1.0
+    dt: float = 0.02
+    beta: float = 0.3
+    wrap: bool = True
+    position_setter: int = 0  # PLG_POS_UNIFORM
+    type_setter: int = 0  # PLG_TYPE_RANDOM
+    seed: int = 0
+
+
+def gen_struct(g: GeneratedWorld, keep: list) -> "_lib.plg_world_gen":
+    m = np.ascontiguousarray(g.matrix, dtype=np.float64)
+    keep.append(m)
+    s = _lib.plg_world_gen()
+    s.world.settings = _lib.plg_settings(g.rmax, g.friction, g.force, g.dt, g.beta, 1 if g.wrap else 0,
+                                         _lib.PLG_ACCEL_PARTICLE_LIFE)
+    s.world.ntypes = m.shape[0]
+    s.world.matrix = _lib.ptr(m, _lib.C.c_double)
+    s.world.n = int(g.n)
+    s.position_setter = int(g.position_setter)
+    s.type_setter = int(g.type_setter)
+    s.seed = int(g.seed)
+    return s
 
 
 def _check(status: int, s, what: str) -> None:
@@ -59,10 +93,37 @@ class Server:
         self._n[rid.value] = int(d.n)
         return rid.value
 
+    def submit_generated(self, dim: int, world: GeneratedWorld, steps: int) -> int:
+        keep: list = []
+        g = gen_struct(world, keep)
+        rid = _lib.C.c_int64()
+        _check(self.lib.plg_server_submit_generated(self.s, dim, _lib.C.byref(g), int(steps), _lib.C.byref(rid)),
+               self.s, "plg_server_submit_generated")
+        self._n[rid.value] = int(world.n)
+        return rid.value
+
     def wait(self, rid: int, timeout_s: float = 0.0) -> int:
         st = _lib.C.c_int32()
         _check(self.lib.plg_server_wait(self.s, rid, timeout_s, _lib.C.byref(st)), self.s, "plg_server_wait")
         return st.value
+
+    def wait_any(self, timeout_s: float = 0.0) -> Optional[int]:
+        """The id of a request that finished (each is given once, in
+        completion order), or None when none finished within timeout_s."""
+        rid = _lib.C.c_int64()
+        st = self.lib.plg_server_wait_any(self.s, timeout_s, _lib.C.byref(rid))
+        if st == _lib.PLG_E_TIMEOUT:
+            return None
+        _check(st, self.s, "plg_server_wait_any")
+        return rid.value
+
+    def release(self, rid: int) -> float:
+        """Drops a finished request's result; returns its latency in ms."""
+        self._n.pop(rid, None)
+        lat = _lib.C.c_double()
+        _check(self.lib.plg_server_result(self.s, rid, None, None, None, None, None, _lib.C.byref(lat)), self.s,
+               "plg_server_result")
+        return lat.value
 
     def result(self, rid: int):
         """(pos, vel, types, ids, latency_ms) of a finished request."""
@@ -81,7 +142,9 @@ class Server:
     def stats(self) -> dict:
         st = _lib.plg_server_stats_t()
         _check(self.lib.plg_server_stats(self.s, _lib.C.byref(st)), self.s, "plg_server_stats")
-        return {name: getattr(st, name) for name, _ in st._fields_}
+        out = {name: getattr(st, name) for name, _ in st._fields_}
+        out["busy_dim_s"] = list(st.busy_dim_s)
+        return out
 
     @staticmethod
     def device_bytes(dim: int, world: WorldDesc) -> int:

@@ -68,6 +68,32 @@ def serving_request(rng: np.random.Generator, n_lo: int = 1_000, n_hi: int = 2_0
     return dim, random_world(rng, dim, n, ntypes, rmax, friction_of_half_life(0.043), 0.02), steps
 
 
+def serving_request_generated(rng: np.random.Generator, n_lo: int = 1_000, n_hi: int = 2_000_000,
+                              steps_lo: int = 100, steps_hi: int = 5_000):
+    """One request of the served configuration as a world spec the server
+    generates on the device: the distributions of serving_request (2D or 3D
+    50/50, N log-uniform in [n_lo, n_hi], types uniform in 3..16, matrix
+    uniform in [-1,1], rmax for k uniform in [10, 50] neighbours, friction
+    half-life 0.043 s, dt 0.02, steps uniform in [steps_lo, steps_hi]),
+    positions uniform and types uniform from a per-request seed."""
+    from .serve import GeneratedWorld
+
+    dim = 2 if rng.random() < 0.5 else 3
+    n = int(round(math.exp(rng.uniform(math.log(n_lo), math.log(n_hi)))))
+    ntypes = int(rng.integers(3, 17))
+    k = float(rng.uniform(10, 50))
+    if dim == 2:
+        rmax = math.sqrt(k / (math.pi * n))
+    else:
+        rmax = (3 * k / (4 * math.pi * n)) ** (1 / 3)
+    rmax = min(rmax, 0.3)
+    steps = int(rng.integers(steps_lo, steps_hi + 1))
+    m = np.asarray(2 * rng.random((ntypes, ntypes)) - 1, np.float32).astype(np.float64)
+    seed = int(rng.integers(0, 2**63))
+    return dim, GeneratedWorld(n=n, matrix=m, rmax=rmax, friction=friction_of_half_life(0.043), dt=0.02,
+                               seed=seed), steps
+
+
 # rmax of the 3D blob configuration: bisection (30 halvings) of the mean
 # neighbour count within rmax over a 1% sample of the 4M-particle world below
 # (periodic KD-tree), to 40 neighbours.

@@ -98,3 +98,82 @@ def test_rejections_and_zero_steps(gpu):
     srv.close()
     assert np.array_equal(ids, np.arange(3_000))
     assert np.array_equal(pos, w.pos) and np.array_equal(types, w.types)
+
+
+def alone_generated(dim, g, steps):
+    from plgpu.physics import GpuWorld
+
+    w = GpuWorld(dim, max(g.n, 1))
+    w.set_settings(g.rmax, g.friction, g.force, g.dt, beta=g.beta, wrap=g.wrap)
+    w.set_matrix(g.matrix)
+    w.generate(g.n, g.position_setter, g.type_setter, g.seed)
+    w.step(steps)
+    out = w.download()
+    w.close()
+    return out
+
+
+def test_large_worlds_equal_the_world_run_alone(gpu):
+    """A 1M-particle 2D world (20 neighbours, uploaded) and a 3D world at 50
+    neighbours (generated on the device), each served while small worlds
+    arrive, finish and leave around them, end bit for bit where they end
+    alone."""
+    import math
+
+    from plgpu import workloads
+    from plgpu.serve import GeneratedWorld, Server
+
+    rng = np.random.Generator(np.random.Philox(94))
+    big2 = workloads.random_world(rng, 2, 1_000_000, 8, math.sqrt(20 / (math.pi * 1e6)), 0.7644, 0.01)
+    m3 = np.asarray(2 * rng.random((12, 12)) - 1, np.float32).astype(np.float64)
+    big3 = GeneratedWorld(n=300_000, matrix=m3, rmax=(3 * 50 / (4 * math.pi * 3e5)) ** (1 / 3), friction=0.7644,
+                          dt=0.02, seed=5)
+    small = requests(8, seed=95, n_hi=20_000, steps_hi=12)
+    srv = Server(memory_budget_bytes=8 << 30, particle_capacity=(4_000_000, 2_000_000),
+                 cell_capacity=(4_000_000, 4_000_000), max_chunk_steps=3)
+    ids = [srv.submit(2, big2, 7), srv.submit_generated(3, big3, 5)]
+    for dim, w, steps in small:
+        ids.append(srv.submit(dim, w, steps))
+        time.sleep(0.003)
+    for rid in ids:
+        srv.wait(rid, 120.0)
+    results = [srv.result(rid) for rid in ids]
+    st = srv.stats()
+    srv.close()
+    assert st["completed"] == len(ids)
+    refs = [alone(2, big2, 7), alone_generated(3, big3, 5)] + [alone(dim, w, steps) for dim, w, steps in small]
+    for ref, got in zip(refs, results):
+        for a, c in zip(ref, got[:4]):
+            assert np.array_equal(a, c)
+
+
+def test_generated_requests_and_compaction(gpu):
+    """Generated worlds through a server whose batches hold only a few
+    worlds: finished worlds must be compacted away to admit the rest; every
+    result equals plg_generate + plg_step in a single-world context."""
+    from plgpu import workloads
+    from plgpu.serve import Server
+
+    rng = np.random.Generator(np.random.Philox(96))
+    reqs = [workloads.serving_request_generated(rng, n_lo=2_000, n_hi=30_000, steps_lo=1, steps_hi=20)
+            for _ in range(14)]
+    srv = Server(memory_budget_bytes=4 << 30, particle_capacity=(70_000, 70_000),
+                 cell_capacity=(2_000_000, 2_000_000), max_chunk_steps=4)
+    ids = []
+    for dim, g, steps in reqs:
+        ids.append(srv.submit_generated(dim, g, steps))
+        time.sleep(0.002)
+    seen = set()
+    while len(seen) < len(ids):
+        rid = srv.wait_any(60.0)
+        assert rid is not None
+        seen.add(rid)
+    results = [srv.result(rid) for rid in ids]
+    st = srv.stats()
+    srv.close()
+    assert st["completed"] == len(ids) and st["compactions"] > 0
+    assert st["busy_s"] > 0 and st["resident_bytes"] == 0
+    for (dim, g, steps), got in zip(reqs, results):
+        ref = alone_generated(dim, g, steps)
+        for a, c in zip(ref, got[:4]):
+            assert np.array_equal(a, c)
