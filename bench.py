@@ -301,7 +301,7 @@ def run_batched(args) -> dict:
     b.update(add=worlds)
     stream = torch.cuda.ExternalStream(b.stream())
     b.step(args.warmup)
-    variant, tune_ms = b.autotune(3)
+    choice, tune_ms = b.autotune_worlds(2)  # per world; state restored
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
           for _ in range(args.batched_steps)]
     torch.cuda.synchronize()
@@ -334,7 +334,9 @@ def run_batched(args) -> dict:
             "one_at_a_time": {"value": single, "unit": UNIT,
                               "how": "each world in its own context, plg_step(K) in turn, host wall clock"},
             "speedup_vs_one_at_a_time": batched / single,
-            "autotune": {"chosen_tile_variant": variant, "ms_per_step_by_variant": tune_ms},
+            "autotune": {"per_world": True,
+                         "worlds_by_variant": {str(v): sum(1 for x in choice.values() if x == v) for v in (0, 1)},
+                         "ms_per_step": {"variant_0": tune_ms[0], "variant_1": tune_ms[1], "mixed": tune_ms[2]}},
             "config": "512 2D periodic worlds, N log-uniform [1e3, 2e5], types 3..12, rmax U[0.005, 0.03] "
                       "(unit box), friction t1/2 U[0.02, 0.1] s, dt 0.02; seeded Philox"}
 
@@ -448,7 +450,7 @@ def run_serving(args) -> dict:
     cap = (int(args.serve_cap_2d), int(args.serve_cap_3d))
     cells = (int(args.serve_cells_2d), int(args.serve_cells_3d))
     srv = Server(memory_budget_bytes=150 << 30, particle_capacity=cap, cell_capacity=cells,
-                 max_worlds_per_batch=1024, max_chunk_steps=16)
+                 max_worlds_per_batch=1024, max_chunk_steps=16, autotune_interval_ms=2000)
     stop = threading.Event()
 
     def collect():  # hands every finished result back to the host and drops it
@@ -508,7 +510,7 @@ def run_serving(args) -> dict:
             "latency_mean_ms": st["latency_mean_ms"],
             "value": served, "unit": UNIT, "offered_particle_steps_per_s": offered,
             "device_busy_fraction": {"2d": st["busy_dim_s"][0] / wall, "3d": st["busy_dim_s"][1] / wall},
-            "compactions": st["compactions"],
+            "compactions": st["compactions"], "autotunes": st["autotunes"],
             "one_at_a_time": {"value": alone, "unit": UNIT, "requests": alone_n,
                               "how": "the first requests in arrival order, each generated alone in a single-world "
                                      "context, min(steps, 100) steps timed (host wall clock) and scaled to its step "
@@ -519,7 +521,7 @@ def run_serving(args) -> dict:
                       f"{args.serve_drain_s:g} s of drain), 2D/3D 50/50, N log-uniform [1e3, 2e6], types 3..16, "
                       "k U[10, 50], steps U[100, 5000], worlds generated on the device (uniform positions and "
                       f"types, seeded), budget 150 GB, batch capacities {cap[0]:,} (2D) / {cap[1]:,} (3D) "
-                      "particles, chunks of <= 16 steps; seeded Philox"}
+                      "particles, chunks of <= 16 steps, per-world tile tuning every 2 s; seeded Philox"}
 
 
 def run_reference(args):

@@ -417,19 +417,37 @@ int plg_batch_get_stream(plg_batch* batch, void** stream);
 const char* plg_batch_last_error(plg_batch* batch);
 int plg_batch_step_stats(plg_batch* batch, int64_t* deferred);
 /* Force kernel tile variants (threads = targets per block, staging size):
- * 2D: 0 = 128 targets / 1024 staged candidates, 1 = 128 / 2560;
- * 3D: 0 = 128 / 2048, 1 = 64 / 1024.  Both give the same bits.  The
- * cell size is not a tuning choice: it is rmax (the sorted order the
- * reference exposes depends on it).  A single world has the same choice:
- * plg_set_tile / plg_autotune. */
+ * 2D: 0 = 128 targets / 1280 staged candidates, 1 = 128 / 3072;
+ * 3D: 0 = 128 / 2048, 1 = 64 / 1024.  Both give the same bits.  Each world
+ * of a batch has its own variant; a step launches the force kernel once per
+ * variant in use.  The cell size is not a tuning choice: it is rmax (the
+ * sorted order the reference exposes depends on it).  A single world has
+ * the same choice: plg_set_tile / plg_autotune. */
 #define PLG_TILE_VARIANTS 2
+/* Every world (and every world added later) takes `variant`. */
 int plg_batch_set_tile(plg_batch* batch, int32_t variant);
 int plg_batch_get_tile(plg_batch* batch, int32_t* variant);
-/* Autotuner: times `steps` steps of every tile variant on the batch as it
- * is (restoring the particle state after each trial, so no world moves),
- * keeps the fastest and reports it; ms_per_step (may be NULL) receives
+/* One world's variant. */
+int plg_batch_set_world_tile(plg_batch* batch, int32_t id, int32_t variant);
+int plg_batch_get_world_tile(plg_batch* batch, int32_t id, int32_t* variant);
+/* The ids of the batch's worlds in device order (plg_batch_counts gives
+ * their number). */
+int plg_batch_world_ids(plg_batch* batch, int32_t* ids);
+/* Autotuner, one variant for the batch: times `steps` steps of every tile
+ * variant on the batch as it is (restoring the state after each trial, so
+ * no world moves and no step budget is spent), gives every world the
+ * fastest and reports it; ms_per_step (may be NULL) receives
  * PLG_TILE_VARIANTS times.  Allocates a temporary copy of the state. */
 int plg_batch_autotune(plg_batch* batch, int32_t steps, int32_t* chosen, double* ms_per_step);
+/* Autotuner, one variant per world: a trial per variant measures each
+ * world's force-kernel SM time (its blocks' cycles over the variant's
+ * resident blocks per SM); every world takes its cheapest variant, and the
+ * resulting mix is kept only if it times faster than the best single
+ * variant (else every world takes that).  State restored as above.
+ * ms_by_variant (may be NULL): PLG_TILE_VARIANTS + 1 step times (each
+ * variant alone, then the mix); variants (may be NULL): each world's
+ * choice in plg_batch_world_ids order. */
+int plg_batch_autotune_worlds(plg_batch* batch, int32_t steps, int32_t* variants, double* ms_by_variant);
 
 /* plg_debug_step over the whole batch: per sorted slot (worlds one after
  * another), cell = global cell index (world's first cell + its own). */
@@ -461,7 +479,10 @@ typedef struct plg_server_config {
     int64_t cell_capacity[2];
     int32_t max_worlds_per_batch;  /* <= 1024 */
     int32_t max_chunk_steps;       /* steps between admissions */
-    int32_t tile_variant;          /* force kernel tile variant, fixed for the server's life */
+    int32_t tile_variant;          /* force kernel tile variant of newly admitted worlds */
+    int32_t autotune_interval_ms;  /* > 0: at a chunk boundary at least this long after the last,
+                                      re-tune the batch per world (plg_batch_autotune_worlds, one
+                                      step per trial; results do not change); 0: off */
 } plg_server_config;
 
 #define PLG_REQ_QUEUED 0
@@ -476,6 +497,7 @@ typedef struct plg_server_stats_t {
     double latency_p50_ms, latency_p99_ms, latency_mean_ms;  /* submit -> result on host */
     double busy_dim_s[2];    /* device time of the step chunks of the 2D and of the 3D batch */
     int64_t compactions;     /* re-layout passes that dropped finished worlds */
+    int64_t autotunes;       /* per-world tuner runs */
 } plg_server_stats_t;
 
 int plg_server_create(const plg_server_config* cfg, plg_server** out);

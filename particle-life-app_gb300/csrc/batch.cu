@@ -44,6 +44,7 @@ struct WorldRec {
     int64_t p_off = 0, c_off = 0, m_off = 0, b_off = 0;
     int32_t steps_left = INT32_MAX;  // steps before the world freezes (INT32_MAX: no limit)
     bool dead = false;               // retired: frozen in place until the next compaction
+    int variant = 0;                 // force kernel tile variant of this world
 };
 
 }  // namespace
@@ -103,7 +104,10 @@ struct plg_batch {
     unsigned char* side_stage = nullptr;  // staging of tail conversions and downloads
     int64_t side_stage_cap = 0;
     int32_t next_id = 1;
-    int variant = 0;  // force kernel tile variant (autotuner)
+    int variant = 0;  // tile variant given to new worlds (plg_batch_set_tile sets every world's)
+    unsigned long long* wcycles_d = nullptr;  // wcap: per-world block cycles (per-world autotuner)
+    void* tune_save[5] = {};                  // the tuners' copy of the state (kept, grown on demand)
+    size_t tune_cap[5] = {};
     int64_t n_total = 0, c_total = 0;
     bool smem_matrix = true;
 
@@ -195,8 +199,10 @@ void free_batch(plg_batch* b) {
                     b->status_d, b->worlds_d,  b->wp_off_d,  b->move_new_d,  b->move_old_d, b->bounds_d,
                     b->tile_off_d, b->steps_left_d,
                     b->matrix_d, b->stage,     b->dbg_pairs, b->dbg_hsum,    b->dbg_hxor, b->dbg_cand,
-                    b->dbg_acc,  b->dbg_cell,  b->side_stage};
+                    b->dbg_acc,  b->dbg_cell,  b->side_stage, b->wcycles_d};
     for (void* p : ptrs)
+        if (p) cudaFree(p);
+    for (void* p : b->tune_save)
         if (p) cudaFree(p);
     if (b->status_h) cudaFreeHost(b->status_h);
     if (b->stream) cudaStreamDestroy(b->stream);
@@ -261,6 +267,29 @@ int check_desc(plg_batch* b, const plg_world_desc& d) {
     return rc ? berr(b, rc, msg) : PLG_OK;
 }
 
+// The force kernel's tile tables: for each variant v, the first tile of
+// every world in the launch of v's worlds (a world of another variant has
+// no tiles there).  A block never spans two worlds, and every world is cut
+// into exactly the tiles a single-world launch of its variant uses.
+int write_tiles(plg_batch* b) {
+    const size_t nw = b->worlds.size();
+    std::vector<int> toff((size_t)PLG_TILE_VARIANTS * (b->wcap + 1), 0);
+    for (int v = 0; v < PLG_TILE_VARIANTS; ++v) {
+        const int kt = tile_targets(b->dim, v);
+        int t = 0;
+        for (size_t k = 0; k < nw; ++k) {
+            toff[(size_t)v * (b->wcap + 1) + k] = t;
+            if (b->worlds[k].variant == v) t += (int)((b->worlds[k].n + kt - 1) / kt);
+        }
+        toff[(size_t)v * (b->wcap + 1) + nw] = t;
+        b->tiles[v] = t;
+    }
+    BCK(b, cudaMemcpyAsync(b->tile_off_d, toff.data(), sizeof(int) * toff.size(), cudaMemcpyHostToDevice, b->stream));
+    BCK(b, cudaStreamSynchronize(b->stream));
+    destroy_batch_graph(b);
+    return PLG_OK;
+}
+
 // Writes the device world tables for the current b->worlds layout.
 int upload_tables(plg_batch* b) {
     const size_t nw = b->worlds.size();
@@ -292,29 +321,16 @@ int upload_tables(plg_batch* b) {
         if (w.ntypes > 16) b->smem_matrix = false;
     }
     off[nw] = (int)b->n_total;
-    // Tiles of each world for every variant: a block never spans two worlds.
-    std::vector<int> toff((size_t)PLG_TILE_VARIANTS * (b->wcap + 1), 0);
-    for (int v = 0; v < PLG_TILE_VARIANTS; ++v) {
-        const int kt = tile_targets(b->dim, v);
-        int t = 0;
-        for (size_t k = 0; k < nw; ++k) {
-            toff[(size_t)v * (b->wcap + 1) + k] = t;
-            t += (int)((b->worlds[k].n + kt - 1) / kt);
-        }
-        toff[(size_t)v * (b->wcap + 1) + nw] = t;
-        b->tiles[v] = t;
-    }
     if (nb) BCK(b, cudaMemcpyAsync(b->bounds_d, bounds.data(), sizeof(float) * nb, cudaMemcpyHostToDevice, b->stream));
     if (nm) BCK(b, cudaMemcpyAsync(b->matrix_d, matrix.data(), sizeof(float) * nm, cudaMemcpyHostToDevice, b->stream));
     if (nw) BCK(b, cudaMemcpyAsync(b->worlds_d, fp.data(), sizeof(ForceParams) * nw, cudaMemcpyHostToDevice, b->stream));
     BCK(b, cudaMemcpyAsync(b->wp_off_d, off.data(), sizeof(int) * (nw + 1), cudaMemcpyHostToDevice, b->stream));
-    BCK(b, cudaMemcpyAsync(b->tile_off_d, toff.data(), sizeof(int) * toff.size(), cudaMemcpyHostToDevice, b->stream));
     std::vector<int> left(std::max<size_t>(nw, 1));
     for (size_t k = 0; k < nw; ++k) left[k] = b->worlds[k].steps_left;
     if (nw) BCK(b, cudaMemcpyAsync(b->steps_left_d, left.data(), sizeof(int) * nw, cudaMemcpyHostToDevice, b->stream));
     // The host vectors die at return: wait for the copies.
     BCK(b, cudaStreamSynchronize(b->stream));
-    return PLG_OK;
+    return write_tiles(b);
 }
 
 template <int D>
@@ -345,6 +361,7 @@ int relayout(plg_batch* b, const std::vector<int>& survivors, const plg_world_de
         const plg_world_desc& d = add[a];
         WorldRec w;
         w.id = b->next_id++;
+        w.variant = b->variant;
         w.n = d.n;
         w.ntypes = d.ntypes;
         w.s = d.settings;
@@ -442,20 +459,31 @@ int relayout(plg_batch* b, const std::vector<int>& survivors, const plg_world_de
     return PLG_OK;
 }
 
+// wcycles (may be null): per-world block cycles of the force launches.
 template <int D>
-void enqueue_batch_step(plg_batch* b, const DebugOut* dbg, int32_t* cell_sorted) {
+void enqueue_batch_step(plg_batch* b, const DebugOut* dbg, int32_t* cell_sorted,
+                        unsigned long long* wcycles = nullptr) {
     cudaStream_t st = b->stream;
     const int n = (int)b->n_total;
     const int nc = (int)std::max<int64_t>(b->c_total, 1);
-    cudaMemsetAsync(b->scan_state, 0, sizeof(unsigned long long) * (size_t)(scan_blocks(nc) + 1), st);
+    // The scan's state starts at zero: the scatter sets it back after each
+    // scan (the whole state was zeroed at creation); with no particles a
+    // memset does it.
+    const int nstate = scan_blocks(nc) + 1;
     launch_scan(st, b->counts, nc, b->cstart, b->scan_state, b->status_d, b->defer);
-    launch_scatter(st, n, b->cell, b->counts, b->cstart, b->perm, b->slot_cell);
+    if (n > 0)
+        launch_scatter(st, n, b->cell, b->counts, b->cstart, b->perm, b->slot_cell, b->scan_state, nstate);
+    else
+        cudaMemsetAsync(b->scan_state, 0, sizeof(unsigned long long) * (size_t)nstate, st);
     launch_gather<D>(st, n, b->perm, b->slot_cell, b->cstart, sbuf<D>(b->apt, b->avel, 0),
                      sbuf<D>(b->bpt, b->bvel, 0), cell_sorted);
-    launch_force_batch<D>(st, b->worlds_d, b->wp_off_d, b->tile_off_d + (size_t)b->variant * (b->wcap + 1),
-                          b->steps_left_d, b->tiles[b->variant], (int)b->worlds.size(), n, b->smem_matrix,
-                          sbuf<D>(b->bpt, b->bvel, 0), b->cstart, b->slot_cell, sbuf<D>(b->apt, b->avel, 0), b->cell,
-                          b->counts, b->defer, dbg, b->variant);
+    // One force launch per tile variant in use; the launches touch disjoint
+    // worlds.
+    for (int v = 0; v < PLG_TILE_VARIANTS; ++v)
+        launch_force_batch<D>(st, b->worlds_d, b->wp_off_d, b->tile_off_d + (size_t)v * (b->wcap + 1),
+                              b->steps_left_d, b->tiles[v], (int)b->worlds.size(), n, b->smem_matrix,
+                              sbuf<D>(b->bpt, b->bvel, 0), b->cstart, b->slot_cell, sbuf<D>(b->apt, b->avel, 0),
+                              b->cell, b->counts, b->defer, dbg, v, wcycles);
     launch_batch_tick(st, b->steps_left_d, (int)b->worlds.size());
 }
 
@@ -535,6 +563,7 @@ template <int D>
 int append_world(plg_batch* b, const plg_world_desc& d, const WorldGen* gen, int32_t steps, cudaStream_t side,
                  int32_t* id_out) {
     WorldRec w;
+    w.variant = b->variant;
     w.n = d.n;
     w.ntypes = d.ntypes;
     w.s = d.settings;
@@ -839,6 +868,9 @@ int plg_batch_create(int32_t dim, int64_t particle_capacity, int32_t world_capac
     if (!rc && cudaMallocHost((void**)&b->status_h, 64) != cudaSuccess) rc = PLG_E_NO_MEMORY;
     if (!rc && cudaMemset(b->status_d, 0, 64) != cudaSuccess) rc = PLG_E_CUDA;
     if (!rc && cudaMemset(b->counts, 0, sizeof(uint32_t) * cc) != cudaSuccess) rc = PLG_E_CUDA;
+    if (!rc && cudaMemset(b->scan_state, 0, sizeof(unsigned long long) * (size_t)(scan_blocks((int)cc) + 1)) !=
+                   cudaSuccess)
+        rc = PLG_E_CUDA;
     if (rc) {
         cudaGetLastError();
         free_batch(b);
@@ -971,9 +1003,11 @@ int plg_batch_download(plg_batch* b, int32_t id, double* pos, double* vel, int32
 int plg_batch_set_tile(plg_batch* b, int32_t variant) {
     if (!b) return PLG_E_INVALID_ARG;
     if (variant < 0 || variant >= PLG_TILE_VARIANTS) return berr(b, PLG_E_INVALID_ARG, "unknown tile variant");
-    if (variant != b->variant) destroy_batch_graph(b);
+    BatchDeviceGuard g(b->device);
     b->variant = variant;
-    return PLG_OK;
+    for (WorldRec& w : b->worlds) w.variant = variant;
+    for (WorldRec& w : b->pending) w.variant = variant;
+    return write_tiles(b);
 }
 
 int plg_batch_get_tile(plg_batch* b, int32_t* variant) {
@@ -982,81 +1016,242 @@ int plg_batch_get_tile(plg_batch* b, int32_t* variant) {
     return PLG_OK;
 }
 
+int plg_batch_set_world_tile(plg_batch* b, int32_t id, int32_t variant) {
+    if (!b) return PLG_E_INVALID_ARG;
+    if (variant < 0 || variant >= PLG_TILE_VARIANTS) return berr(b, PLG_E_INVALID_ARG, "unknown tile variant");
+    const int k = find_world(b, id);
+    if (k < 0) return berr(b, PLG_E_INVALID_ARG, "unknown world id " + std::to_string(id));
+    if (b->worlds[(size_t)k].variant == variant) return PLG_OK;
+    BatchDeviceGuard g(b->device);
+    b->worlds[(size_t)k].variant = variant;
+    return write_tiles(b);
+}
+
+int plg_batch_get_world_tile(plg_batch* b, int32_t id, int32_t* variant) {
+    if (!b || !variant) return PLG_E_INVALID_ARG;
+    const int k = find_world(b, id);
+    if (k < 0) return berr(b, PLG_E_INVALID_ARG, "unknown world id " + std::to_string(id));
+    *variant = b->worlds[(size_t)k].variant;
+    return PLG_OK;
+}
+
+namespace {
+
+// The state a trial step changes (A, the next cells and their counts, the
+// worlds' step budgets), copied aside and put back, so that a tuner's
+// trials leave the batch where it was.  The copy lives in the batch
+// (allocated on first use, grown when the batch has grown), so a tuner
+// called again, as the serving loop does, allocates nothing.  A and B swap
+// only in a re-layout, so the live pointers stay valid across the trials.
+struct TrialState {
+    static constexpr int kParts = 5;
+    plg_batch* b;
+    void* live[kParts] = {};
+    void* save[kParts] = {};
+    size_t bytes[kParts] = {};
+    explicit TrialState(plg_batch* bb) : b(bb) {
+        const size_t n = (size_t)b->n_total, nc = (size_t)std::max<int64_t>(b->c_total, 1);
+        const size_t vel_sz = b->dim == 2 ? sizeof(float2) : sizeof(float4);
+        const size_t by[kParts] = {sizeof(float4) * n, vel_sz * n, 4 * n, 4 * nc,
+                                   sizeof(int) * std::max<size_t>(b->worlds.size(), 1)};
+        void* lv[kParts] = {b->apt, b->avel, b->cell, b->counts, b->steps_left_d};
+        for (int k = 0; k < kParts; ++k) {
+            bytes[k] = by[k];
+            live[k] = lv[k];
+        }
+    }
+    int alloc() {
+        for (int k = 0; k < kParts; ++k) {
+            if (b->tune_cap[k] < bytes[k]) {
+                if (b->tune_save[k]) {
+                    BCK(b, cudaStreamSynchronize(b->stream));
+                    cudaFree(b->tune_save[k]);
+                }
+                b->tune_save[k] = nullptr;
+                b->tune_cap[k] = 0;
+                if (cudaMalloc(&b->tune_save[k], bytes[k]) != cudaSuccess) {
+                    cudaGetLastError();
+                    b->tune_save[k] = nullptr;
+                    return berr(b, PLG_E_NO_MEMORY, "cudaMalloc (tuner state copy)");
+                }
+                b->tune_cap[k] = bytes[k];
+            }
+            save[k] = b->tune_save[k];
+        }
+        return PLG_OK;
+    }
+    int copy(bool restore) {
+        for (int k = 0; k < kParts; ++k)
+            BCK(b, cudaMemcpyAsync(restore ? live[k] : save[k], restore ? save[k] : live[k], bytes[k],
+                                   cudaMemcpyDeviceToDevice, b->stream));
+        return PLG_OK;
+    }
+};
+
+// `steps` timed steps of the batch as it is (one untimed step first builds
+// the graph), then the state restored; *ms: per step.  With wcycles, the
+// steps run as plain launches and each world's force-kernel block cycles
+// are summed there.
+int trial(plg_batch* b, TrialState& ts, int32_t steps, double* ms, unsigned long long* wcycles) {
+    cudaStream_t st = b->stream;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    int rc = PLG_OK;
+    if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) rc = bcuda(b, "event", cudaGetLastError());
+    if (!rc && wcycles) {
+        if (cudaMemsetAsync(wcycles, 0, sizeof(unsigned long long) * b->worlds.size(), st) != cudaSuccess)
+            rc = bcuda(b, "cudaMemsetAsync", cudaGetLastError());
+        if (!rc && cudaEventRecord(e0, st) != cudaSuccess) rc = bcuda(b, "event", cudaGetLastError());
+        for (int32_t k = 0; k < steps && !rc; ++k) {
+            if (b->dim == 2)
+                enqueue_batch_step<2>(b, nullptr, nullptr, wcycles);
+            else
+                enqueue_batch_step<3>(b, nullptr, nullptr, wcycles);
+            if (cudaGetLastError() != cudaSuccess) rc = berr(b, PLG_E_CUDA, "tuner step launch");
+        }
+    } else if (!rc) {
+        rc = enqueue_step(b);  // builds the graph, untimed
+        if (!rc && cudaEventRecord(e0, st) != cudaSuccess) rc = bcuda(b, "event", cudaGetLastError());
+        for (int32_t k = 0; k < steps && !rc; ++k) rc = enqueue_step(b);
+    }
+    float t = 0.f;
+    if (!rc && (cudaEventRecord(e1, st) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
+                cudaEventElapsedTime(&t, e0, e1) != cudaSuccess))
+        rc = bcuda(b, "tuner timing", cudaGetLastError());
+    if (!rc) rc = ts.copy(true);
+    if (!rc && cudaStreamSynchronize(st) != cudaSuccess) rc = bcuda(b, "tuner", cudaGetLastError());
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (ms) *ms = t / steps;
+    return rc;
+}
+
+void set_all_variants(plg_batch* b, int v) {
+    for (WorldRec& w : b->worlds) w.variant = v;
+}
+
+}  // namespace
+
 // Times `steps` steps of each tile variant on the batch as it is, restoring
-// the particle state after each trial, and keeps the fastest variant.  The
-// trials allocate a copy of the state and free it before returning.
+// the particle state after each trial, and gives every world the fastest
+// variant.  The trials allocate a copy of the state and free it before
+// returning.
 int plg_batch_autotune(plg_batch* b, int32_t steps, int32_t* chosen, double* ms_per_step) {
     if (!b) return PLG_E_INVALID_ARG;
     if (steps < 1) return berr(b, PLG_E_INVALID_ARG, "autotune needs at least one step");
+    if (!b->pending.empty()) return berr(b, PLG_E_STATE, "worlds appended to the tail are not committed yet");
     BatchDeviceGuard g(b->device);
-    cudaStream_t st = b->stream;
-    const size_t n = (size_t)b->n_total, nc = (size_t)std::max<int64_t>(b->c_total, 1);
-    if (n == 0) {
+    if (b->n_total == 0) {
         if (chosen) *chosen = b->variant;
         return PLG_OK;
     }
-    const size_t vel_sz = b->dim == 2 ? sizeof(float2) : sizeof(float4);
-    const size_t bytes[4] = {sizeof(float4) * n, vel_sz * n, 4 * n, 4 * nc};
-    void* live[4] = {b->apt, b->avel, b->cell, b->counts};
-    void* save[4] = {};
-    int rc = PLG_OK;
-    for (int k = 0; k < 4 && !rc; ++k)
-        if (cudaMalloc(&save[k], bytes[k]) != cudaSuccess) {
-            cudaGetLastError();
-            rc = berr(b, PLG_E_NO_MEMORY, "cudaMalloc (autotune state copy)");
-        }
-    auto copy_all = [&](bool restore) -> cudaError_t {
-        for (int k = 0; k < 4; ++k) {
-            // A and B swap only in plg_batch_update, so `live` stays valid.
-            cudaError_t e = cudaMemcpyAsync(restore ? live[k] : save[k], restore ? save[k] : live[k], bytes[k],
-                                            cudaMemcpyDeviceToDevice, st);
-            if (e != cudaSuccess) return e;
-        }
-        return cudaSuccess;
-    };
-    cudaEvent_t e0 = nullptr, e1 = nullptr;
-    if (!rc && (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)) rc = PLG_E_CUDA;
-    if (!rc && copy_all(false) != cudaSuccess) rc = bcuda(b, "autotune save", cudaGetLastError());
+    std::vector<int> before;
+    for (const WorldRec& w : b->worlds) before.push_back(w.variant);
+    TrialState ts(b);
+    int rc = ts.alloc();
+    if (!rc) rc = ts.copy(false);
     const int old = b->variant;
-    double best = 1e300;
     double times[PLG_TILE_VARIANTS] = {};
     int best_v = old;
+    double best = 1e300;
     for (int v = 0; v < PLG_TILE_VARIANTS && !rc; ++v) {
-        if (v != b->variant) destroy_batch_graph(b);
-        b->variant = v;
-        if ((rc = enqueue_step(b))) break;  // builds the graph, untimed
-        if (cudaEventRecord(e0, st) != cudaSuccess) rc = PLG_E_CUDA;
-        for (int32_t k = 0; k < steps && !rc; ++k) rc = enqueue_step(b);
-        if (rc) break;
-        float ms = 0.f;
-        if (cudaEventRecord(e1, st) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
-            cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) {
-            rc = bcuda(b, "autotune timing", cudaGetLastError());
-            break;
-        }
-        const double per = ms / steps;
-        if (ms_per_step) ms_per_step[v] = per;
-        times[v] = per;
-        if (per < best) {
-            best = per;
+        set_all_variants(b, v);
+        if ((rc = write_tiles(b))) break;
+        rc = trial(b, ts, steps, &times[v], nullptr);
+        if (ms_per_step) ms_per_step[v] = times[v];
+        if (!rc && times[v] < best) {
+            best = times[v];
             best_v = v;
         }
-        if (copy_all(true) != cudaSuccess) rc = bcuda(b, "autotune restore", cudaGetLastError());
     }
-    if (!rc && cudaStreamSynchronize(st) != cudaSuccess) rc = bcuda(b, "autotune", cudaGetLastError());
-    for (void* p : save)
-        if (p) cudaFree(p);
-    if (e0) cudaEventDestroy(e0);
-    if (e1) cudaEventDestroy(e1);
     if (rc) {
-        b->variant = old;
-        destroy_batch_graph(b);
+        for (size_t k = 0; k < b->worlds.size(); ++k) b->worlds[k].variant = before[k];
+        write_tiles(b);
         return rc;
     }
     best_v = switch_if_faster(old, best_v, times);
-    if (best_v != b->variant) destroy_batch_graph(b);
     b->variant = best_v;
+    set_all_variants(b, best_v);
     if (chosen) *chosen = best_v;
+    return write_tiles(b);
+}
+
+// The per-world tuner.  One trial per variant with every world on it, where
+// each world's force blocks add up their SM cycles; a world's cost under a
+// variant is its cycles divided by the variant's resident blocks per SM (SM
+// time, as the blocks share an SM).  Every world takes its cheapest variant
+// (a world keeps its variant unless another is at least 2% cheaper); the
+// mixed assignment is then timed whole and kept only if it beats the best
+// uniform one, else every world takes that.  ms_by_variant (may be NULL):
+// PLG_TILE_VARIANTS uniform times and the mixed one; variants (may be NULL):
+// each world's choice, in plg_batch_world_ids order.
+int plg_batch_autotune_worlds(plg_batch* b, int32_t steps, int32_t* variants, double* ms_by_variant) {
+    if (!b) return PLG_E_INVALID_ARG;
+    if (steps < 1) return berr(b, PLG_E_INVALID_ARG, "autotune needs at least one step");
+    if (!b->pending.empty()) return berr(b, PLG_E_STATE, "worlds appended to the tail are not committed yet");
+    BatchDeviceGuard g(b->device);
+    const size_t nw = b->worlds.size();
+    if (b->n_total == 0 || nw == 0) return PLG_OK;
+    if (!b->wcycles_d && cudaMalloc((void**)&b->wcycles_d, sizeof(unsigned long long) * b->wcap) != cudaSuccess) {
+        cudaGetLastError();
+        b->wcycles_d = nullptr;
+        return berr(b, PLG_E_NO_MEMORY, "cudaMalloc (tuner cycles)");
+    }
+    std::vector<int> before;
+    for (const WorldRec& w : b->worlds) before.push_back(w.variant);
+    TrialState ts(b);
+    int rc = ts.alloc();
+    if (!rc) rc = ts.copy(false);
+    std::vector<unsigned long long> cyc(nw);
+    std::vector<double> cost((size_t)PLG_TILE_VARIANTS * nw, 0.0);
+    double uni[PLG_TILE_VARIANTS] = {};
+    for (int v = 0; v < PLG_TILE_VARIANTS && !rc; ++v) {
+        set_all_variants(b, v);
+        if ((rc = write_tiles(b))) break;
+        rc = trial(b, ts, steps, nullptr, b->wcycles_d);  // per-world cycles
+        if (!rc && cudaMemcpy(cyc.data(), b->wcycles_d, sizeof(unsigned long long) * nw, cudaMemcpyDeviceToHost) !=
+                       cudaSuccess)
+            rc = bcuda(b, "tuner cycles", cudaGetLastError());
+        if (!rc) rc = trial(b, ts, steps, &uni[v], nullptr);  // the whole batch, as a graph
+        const double per_sm = (double)batch_blocks_per_sm(b->dim, v, b->smem_matrix);
+        for (size_t k = 0; k < nw && !rc; ++k) cost[(size_t)v * nw + k] = (double)cyc[k] / per_sm;
+    }
+    std::vector<int> pick(nw);
+    for (size_t k = 0; k < nw && !rc; ++k) {
+        int best = before[k];
+        for (int v = 0; v < PLG_TILE_VARIANTS; ++v)
+            if (cost[(size_t)v * nw + k] < 0.98 * cost[(size_t)best * nw + k]) best = v;
+        pick[k] = best;
+    }
+    double mixed = 0;
+    if (!rc) {
+        for (size_t k = 0; k < nw; ++k) b->worlds[k].variant = pick[k];
+        rc = write_tiles(b);
+        if (!rc) rc = trial(b, ts, steps, &mixed, nullptr);
+    }
+    if (rc) {
+        for (size_t k = 0; k < nw; ++k) b->worlds[k].variant = before[k];
+        write_tiles(b);
+        return rc;
+    }
+    int best_u = 0;
+    for (int v = 1; v < PLG_TILE_VARIANTS; ++v)
+        if (uni[v] < uni[best_u]) best_u = v;
+    if (mixed > uni[best_u]) {  // the mix lost: every world on the best uniform variant
+        set_all_variants(b, best_u);
+        if ((rc = write_tiles(b))) return rc;
+    }
+    if (ms_by_variant) {
+        for (int v = 0; v < PLG_TILE_VARIANTS; ++v) ms_by_variant[v] = uni[v];
+        ms_by_variant[PLG_TILE_VARIANTS] = mixed;
+    }
+    if (variants)
+        for (size_t k = 0; k < nw; ++k) variants[k] = b->worlds[k].variant;
+    return PLG_OK;
+}
+
+int plg_batch_world_ids(plg_batch* b, int32_t* ids) {
+    if (!b || !ids) return PLG_E_INVALID_ARG;
+    for (size_t k = 0; k < b->worlds.size(); ++k) ids[k] = b->worlds[k].id;
     return PLG_OK;
 }
 

@@ -34,6 +34,7 @@ struct ForceArgs {
     const int* __restrict__ wp_off;
     const int* __restrict__ tile_off;
     const int* __restrict__ steps_left;  // per world; <= 0: frozen this step (may be null)
+    unsigned long long* wcycles;         // per world: SM cycles of its blocks (autotuner; may be null)
     int nworlds;
     int n_total;
 };
@@ -692,6 +693,7 @@ ForceArgs<D> make_args(const ForceParams& p, StateBuf<D> b, const uint32_t* csta
     A.wp_off = nullptr;
     A.tile_off = nullptr;
     A.steps_left = nullptr;
+    A.wcycles = nullptr;
     A.nworlds = 1;
     A.n_total = p.n;
     return A;

@@ -103,6 +103,7 @@ __device__ void general_scan(const ForceArgs<D>& A, const float* Mrow, int s, fl
 
 template <int D, bool DBG, bool SMEM_M>
 __global__ void __launch_bounds__(kThreads) k_force_general(const __grid_constant__ ForceArgs<D> A) {
+    pdl_wait();  // the sort before it
     const ForceParams& P = A.p;
     extern __shared__ float smat[];
     const float* M = P.matrix;
@@ -310,6 +311,7 @@ __global__ void __launch_bounds__(TileCfg<D, V>::kTargets, TileCfg<D, V>::kMinBl
     extern __shared__ __align__(16) unsigned char smraw[];
     TileSmem<D, V>& sm = *reinterpret_cast<TileSmem<D, V>*>(smraw);
     const int tid = threadIdx.x;
+    pdl_wait();  // the sort before it: B, slot_cell, cstart, the drained counts
     int wk = 0, s0 = blockIdx.x * kT, nw = A.p.n;
     if (BATCH) {
         wk = world_of(A.tile_off, A.nworlds, blockIdx.x);
@@ -335,6 +337,8 @@ __global__ void __launch_bounds__(TileCfg<D, V>::kTargets, TileCfg<D, V>::kMinBl
         if (valid) bin_add(A.counts, c, m);
         return;
     }
+    // Autotuner: the block's duration in SM cycles, summed per world.
+    const long long t_start = BATCH && A.wcycles ? clock64() : 0;
     const int nt = P.ntypes, ms = SMEM_M ? smem_matrix_stride<D>(nt) : nt;
     if (SMEM_M) {
         for (int k = tid; k < nt * nt; k += kT) sm.mat[D == 3 ? (k / nt) * ms + k % nt : k] = P.matrix[k];
@@ -501,6 +505,10 @@ __global__ void __launch_bounds__(TileCfg<D, V>::kTargets, TileCfg<D, V>::kMinBl
         fixup_target<D, DBG>(A, P, cs, M, __shfl_sync(kFull, s, src), lane);
     }
     if constexpr (SNAP) write_snapshot_warp<D>(A, s0 + 32 * warp, min(32, nvalid - 32 * warp), lane);
+    if (BATCH && A.wcycles) {  // block-uniform
+        __syncthreads();
+        if (tid == 0) atomicAdd(A.wcycles + wk, (unsigned long long)(clock64() - t_start));
+    }
 }
 
 template <int D, bool DBG, bool BATCH, int V>
@@ -512,16 +520,16 @@ void launch_tile(cudaStream_t st, const ForceArgs<D>& A, bool smem_matrix, int b
     if constexpr (!DBG && !BATCH) {
         if (A.snap.any()) {
             if (smem_matrix)
-                k_force_tile<D, false, true, false, V, true><<<grid, kT, sb, st>>>(A);
+                launch_after(k_force_tile<D, false, true, false, V, true>, dim3(grid), dim3(kT), sb, st, A);
             else
-                k_force_tile<D, false, false, false, V, true><<<grid, kT, sb, st>>>(A);
+                launch_after(k_force_tile<D, false, false, false, V, true>, dim3(grid), dim3(kT), sb, st, A);
             return;
         }
     }
     if (smem_matrix)
-        k_force_tile<D, DBG, true, BATCH, V><<<grid, kT, sb, st>>>(A);
+        launch_after(k_force_tile<D, DBG, true, BATCH, V>, dim3(grid), dim3(kT), sb, st, A);
     else
-        k_force_tile<D, DBG, false, BATCH, V><<<grid, kT, sb, st>>>(A);
+        launch_after(k_force_tile<D, DBG, false, BATCH, V>, dim3(grid), dim3(kT), sb, st, A);
 }
 
 template <int D, bool DBG, bool BATCH>
@@ -540,9 +548,9 @@ void launch_variant(cudaStream_t st, const ForceArgs<D>& A, bool general, int va
         const int grid = (n + kThreads - 1) / kThreads;
         const size_t sb = smem ? sizeof(float) * A.p.ntypes * smem_matrix_stride<D>(A.p.ntypes) : 0;
         if (smem)
-            k_force_general<D, DBG, true><<<grid, kThreads, sb, st>>>(A);
+            launch_after(k_force_general<D, DBG, true>, dim3(grid), dim3(kThreads), sb, st, A);
         else
-            k_force_general<D, DBG, false><<<grid, kThreads, 0, st>>>(A);
+            launch_after(k_force_general<D, DBG, false>, dim3(grid), dim3(kThreads), 0, st, A);
     } else {
         launch_tile_variant<D, DBG, false>(st, A, smem, variant, 0);
     }
@@ -567,7 +575,8 @@ template <int D>
 void launch_force_batch(cudaStream_t st, const ForceParams* worlds, const int* wp_off, const int* tile_off,
                         const int* steps_left, int tiles, int nworlds, int n_total, bool smem_matrix, StateBuf<D> b,
                         const uint32_t* cstart, const uint32_t* slot_cell, StateBuf<D> a, uint32_t* cell,
-                        uint32_t* counts, uint32_t* defer, const DebugOut* dbg, int variant) {
+                        uint32_t* counts, uint32_t* defer, const DebugOut* dbg, int variant,
+                        unsigned long long* wcycles) {
     if (n_total <= 0 || nworlds <= 0 || tiles <= 0) return;
     ForceParams none{};
     ForceArgs<D> A = make_args<D>(none, b, cstart, slot_cell, a, cell, counts, defer, dbg);
@@ -575,12 +584,30 @@ void launch_force_batch(cudaStream_t st, const ForceParams* worlds, const int* w
     A.wp_off = wp_off;
     A.tile_off = tile_off;
     A.steps_left = steps_left;
+    A.wcycles = wcycles;
     A.nworlds = nworlds;
     A.n_total = n_total;
     if (dbg)
         launch_tile_variant<D, true, true>(st, A, smem_matrix, variant, tiles);
     else
         launch_tile_variant<D, false, true>(st, A, smem_matrix, variant, tiles);
+}
+
+// Resident blocks per SM of the batched force kernel of one variant (the
+// autotuner turns block cycles into SM time with it).
+template <int D, int V>
+int batch_blocks_per_sm(bool smem_matrix) {
+    int nb = 0;
+    const cudaError_t e =
+        smem_matrix ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_force_tile<D, false, true, true, V>,
+                                                                   TileCfg<D, V>::kTargets, sizeof(TileSmem<D, V>))
+                    : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_force_tile<D, false, false, true, V>,
+                                                                   TileCfg<D, V>::kTargets, sizeof(TileSmem<D, V>));
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return 1;
+    }
+    return nb > 0 ? nb : 1;
 }
 
 namespace {

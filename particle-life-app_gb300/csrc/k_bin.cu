@@ -268,6 +268,7 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(const uint32_t* __restric
                                                        uint32_t* __restrict__ cstart, unsigned long long* state,
                                                        uint32_t* status, uint32_t* zero_word) {
     __shared__ uint32_t s_tile, s_prefix, total;
+    pdl_release();  // the scatter's blocks may be scheduled as this grid ends
     if (threadIdx.x == 0) s_tile = atomicAdd(reinterpret_cast<unsigned int*>(state), 1u);
     __syncthreads();
     const int tile = (int)s_tile;
@@ -361,7 +362,9 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(const uint32_t* __restric
 constexpr int kScatterPer = 4;
 __global__ void __launch_bounds__(kThreads) k_scatter(int n, const uint32_t* __restrict__ cell, uint32_t* counts,
                                                       const uint32_t* __restrict__ cstart,
-                                                      uint32_t* __restrict__ perm, uint32_t* __restrict__ slot_cell) {
+                                                      uint32_t* __restrict__ perm, uint32_t* __restrict__ slot_cell,
+                                                      unsigned long long* zero_state, int nzero) {
+    pdl_release();
     const int i0 = blockIdx.x * (kThreads * kScatterPer) + threadIdx.x;
     const int lane = threadIdx.x & 31;
     uint32_t c[kScatterPer], top[kScatterPer];
@@ -371,8 +374,11 @@ __global__ void __launch_bounds__(kThreads) k_scatter(int n, const uint32_t* __r
     for (int k = 0; k < kScatterPer; ++k) {
         const int i = i0 + k * kThreads;
         v[k] = i < n;
-        c[k] = v[k] ? cell[i] : 0u;
+        c[k] = v[k] ? cell[i] : 0u;  // written before the scan: needs no wait
     }
+    pdl_wait();  // the scan's offsets, and its reads of the counts, are done
+    if (zero_state && blockIdx.x == 0)
+        for (int k = threadIdx.x; k < nzero; k += kThreads) zero_state[k] = 0ull;
 #pragma unroll
     for (int k = 0; k < kScatterPer; ++k) {
         const unsigned m = __ballot_sync(kFull, v[k]);
@@ -405,6 +411,8 @@ __global__ void __launch_bounds__(kThreads) k_gather(int n, const uint32_t* __re
                                                      const uint32_t* __restrict__ slot_cell,
                                                      const uint32_t* __restrict__ cstart, StateBuf<D> a,
                                                      StateBuf<D> b, int32_t* __restrict__ cell_sorted) {
+    pdl_release();
+    pdl_wait();  // the scatter's perm and slot_cell
     const int s = blockIdx.x * kThreads + threadIdx.x;
     if (s >= n) return;
     const uint32_t i = perm[s];
@@ -481,16 +489,18 @@ void launch_scan(cudaStream_t st, const uint32_t* counts, int ncells, uint32_t* 
 }
 
 void launch_scatter(cudaStream_t st, int n, const uint32_t* cell, uint32_t* counts, const uint32_t* cstart,
-                    uint32_t* perm, uint32_t* slot_cell) {
+                    uint32_t* perm, uint32_t* slot_cell, unsigned long long* zero_state, int nzero) {
     if (n <= 0) return;
-    k_scatter<<<blocks_for(n, kThreads * kScatterPer), kThreads, 0, st>>>(n, cell, counts, cstart, perm, slot_cell);
+    launch_after(k_scatter, dim3(blocks_for(n, kThreads * kScatterPer)), dim3(kThreads), 0, st, n, cell, counts,
+                 cstart, perm, slot_cell, zero_state, nzero);
 }
 
 template <int D>
 void launch_gather(cudaStream_t st, int n, const uint32_t* perm, const uint32_t* slot_cell, const uint32_t* cstart,
                    StateBuf<D> a, StateBuf<D> b, int32_t* cell_sorted) {
     if (n <= 0) return;
-    k_gather<D><<<blocks_for(n, kThreads), kThreads, 0, st>>>(n, perm, slot_cell, cstart, a, b, cell_sorted);
+    launch_after(k_gather<D>, dim3(blocks_for(n, kThreads)), dim3(kThreads), 0, st, n, perm, slot_cell, cstart, a, b,
+                 cell_sorted);
 }
 
 template void launch_upload<2>(cudaStream_t, int, const double*, const double*, const int32_t*, int, StateBuf<2>,

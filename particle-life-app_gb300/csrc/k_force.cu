@@ -18,7 +18,15 @@ int tile_targets(int dim, int variant) {
 
 template void launch_force_batch<2>(cudaStream_t, const ForceParams*, const int*, const int*, const int*, int, int,
                                     int, bool, StateBuf<2>, const uint32_t*, const uint32_t*, StateBuf<2>, uint32_t*,
-                                    uint32_t*, uint32_t*, const DebugOut*, int);
+                                    uint32_t*, uint32_t*, const DebugOut*, int, unsigned long long*);
+
+// k_force3.cu
+int batch_blocks_per_sm_3d(int variant, bool smem_matrix);
+
+int batch_blocks_per_sm(int dim, int variant, bool smem_matrix) {
+    if (dim == 3) return batch_blocks_per_sm_3d(variant, smem_matrix);
+    return variant == 1 ? batch_blocks_per_sm<2, 1>(smem_matrix) : batch_blocks_per_sm<2, 0>(smem_matrix);
+}
 
 template void launch_force<2>(cudaStream_t, const ForceParams&, bool, StateBuf<2>, const uint32_t*, const uint32_t*,
                               StateBuf<2>, uint32_t*, uint32_t*, uint32_t*, const DebugOut*, int,

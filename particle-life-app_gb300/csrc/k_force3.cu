@@ -7,7 +7,11 @@ namespace plg {
 
 template void launch_force_batch<3>(cudaStream_t, const ForceParams*, const int*, const int*, const int*, int, int,
                                     int, bool, StateBuf<3>, const uint32_t*, const uint32_t*, StateBuf<3>, uint32_t*,
-                                    uint32_t*, uint32_t*, const DebugOut*, int);
+                                    uint32_t*, uint32_t*, const DebugOut*, int, unsigned long long*);
+
+int batch_blocks_per_sm_3d(int variant, bool smem_matrix) {
+    return variant == 1 ? batch_blocks_per_sm<3, 1>(smem_matrix) : batch_blocks_per_sm<3, 0>(smem_matrix);
+}
 
 template void launch_force<3>(cudaStream_t, const ForceParams&, bool, StateBuf<3>, const uint32_t*, const uint32_t*,
                               StateBuf<3>, uint32_t*, uint32_t*, uint32_t*, const DebugOut*, int,

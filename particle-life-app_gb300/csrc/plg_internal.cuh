@@ -27,6 +27,36 @@ struct TraceRange {
 
 constexpr unsigned kFull = 0xffffffffu;
 
+// Programmatic dependent launch.  A kernel launched with
+// launch_after (below) may be scheduled while the kernel before it in the
+// stream is still finishing; pdl_wait() returns once that kernel has
+// completed and its writes are visible, so every read of its results comes
+// after it.  Without the launch attribute pdl_wait() returns at once.
+// pdl_release() lets the next kernel's blocks be scheduled as this grid's
+// last blocks run (it orders nothing: the next kernel still waits).
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_release() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
+// Launches kernel<<<grid, block, smem, st>>>(args...) as a programmatic
+// dependent of the work before it in `st` (the kernel must pdl_wait()
+// before it reads that work's results); inside stream capture this becomes
+// a programmatic edge of the graph.
+template <typename... KArgs, typename... Args>
+cudaError_t launch_after(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                         Args... args) {
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
 // Status bits raised by kernels into the context's device status word.
 enum DeviceStatus : uint32_t {
     kDevBadPosition = 1u << 0,  // upload: position outside [0,1] or not finite
@@ -160,9 +190,6 @@ struct ForceParams {
     float m2_inv_rmax;      // -2 / rmax
     float beta_rmax;        // beta * rmax: below this distance the linear repulsion applies
     float k1;               // 1 / (beta * rmax): (|d|/(beta rmax) - 1) / |d| = k1 - 1/|d|
-    float att_k;            // 2 / ((1 - beta) rmax): the triangle's slope per unit distance
-    float att_a0;           // -2 beta / (1 - beta): A = |d| att_k + att_a0 = (s - beta) 2/(1 - beta)
-    float att_b0;           // 2 / (1 - beta):       B = att_b0 - |d| att_k = (1 - s) 2/(1 - beta)
     float ff;               // (float) pow(friction, 60 dt)
     float scale;            // (float) (rmax * force * dt)
     float dt;
@@ -301,8 +328,12 @@ void launch_scan(cudaStream_t st, const uint32_t* counts, int ncells, uint32_t* 
 // perm[cstart[cell[i]] + r] = i with a rank r taken from counts[cell[i]]
 // (bin_take), which leaves counts at zero for the next counting pass.
 // slot_cell (may be null): receives the cell of each sorted slot.
+// zero_state (may be null): nzero words the scan before it used (its tile
+// counter and look-back flags), set back to zero for the next step's scan.
+// A programmatic dependent of the scan (launch_after).
 void launch_scatter(cudaStream_t st, int n, const uint32_t* cell, uint32_t* counts, const uint32_t* cstart,
-                    uint32_t* perm, uint32_t* slot_cell = nullptr);
+                    uint32_t* perm, uint32_t* slot_cell = nullptr, unsigned long long* zero_state = nullptr,
+                    int nzero = 0);
 
 template <int D>
 void launch_gather(cudaStream_t st, int n, const uint32_t* perm, const uint32_t* slot_cell, const uint32_t* cstart,
@@ -327,11 +358,17 @@ void launch_force(cudaStream_t st, const ForceParams& p, bool general, StateBuf<
 // smem_matrix: every world has at most 16 types.
 // steps_left (device, per world, may be null): a world at <= 0 is frozen
 // for the step (its state and order untouched, its cells counted again).
+// wcycles (device, per world, may be null): each block adds its duration in
+// SM cycles to its world's entry (the per-world autotuner).
 template <int D>
 void launch_force_batch(cudaStream_t st, const ForceParams* worlds, const int* wp_off, const int* tile_off,
                         const int* steps_left, int tiles, int nworlds, int n_total, bool smem_matrix, StateBuf<D> b,
                         const uint32_t* cstart, const uint32_t* slot_cell, StateBuf<D> a, uint32_t* cell,
-                        uint32_t* counts, uint32_t* defer, const DebugOut* dbg, int variant = 0);
+                        uint32_t* counts, uint32_t* defer, const DebugOut* dbg, int variant = 0,
+                        unsigned long long* wcycles = nullptr);
+
+// Resident blocks per SM of the batched force kernel of a tile variant.
+int batch_blocks_per_sm(int dim, int variant, bool smem_matrix);
 
 // Counts every positive steps_left[k] (k < nworlds) down by one.
 void launch_batch_tick(cudaStream_t st, int* steps_left, int nworlds);

@@ -66,9 +66,6 @@ void fill_force_params(const plg_settings& s, int nx, int64_t ncells, int ntypes
     p.m2_inv_rmax = (float)(-2.0 / s.rmax);
     p.beta_rmax = (float)(s.beta * s.rmax);
     p.k1 = (float)(1.0 / (s.beta * s.rmax));
-    p.att_k = (float)(2.0 / ((1.0 - s.beta) * s.rmax));
-    p.att_a0 = (float)(-2.0 * s.beta / (1.0 - s.beta));
-    p.att_b0 = (float)(2.0 / (1.0 - s.beta));
     p.ff = (float)std::pow(s.friction, 60 * s.dt);
     p.scale = (float)(s.rmax * s.force * s.dt);
     p.dt = (float)s.dt;
@@ -303,12 +300,18 @@ void enqueue_body(plg_ctx* c, const DebugOut* dbg, int32_t* cell_sorted, const H
     auto k1 = [&](int k) {
         if (c->profiling) cudaEventRecord(c->pev[k][1], st);
     };
+    // The scan's state (tile counter, look-back flags) starts at zero: the
+    // scatter sets it back after each scan; with no particles there is no
+    // scatter, and a memset does it.
+    const int nstate = c->nparts + 1;
     k0(PLG_K_SCAN);
-    cudaMemsetAsync(c->scan_state, 0, sizeof(unsigned long long) * (size_t)(c->nparts + 1), st);
     launch_scan(st, c->counts, c->ncells, c->cstart, c->scan_state, c->status_d, c->general ? nullptr : c->defer);
     k1(PLG_K_SCAN);
     k0(PLG_K_SCATTER);
-    launch_scatter(st, n, c->cell, c->counts, c->cstart, c->perm, c->slot_cell);
+    if (n > 0)
+        launch_scatter(st, n, c->cell, c->counts, c->cstart, c->perm, c->slot_cell, c->scan_state, nstate);
+    else
+        cudaMemsetAsync(c->scan_state, 0, sizeof(unsigned long long) * (size_t)nstate, st);
     k1(PLG_K_SCATTER);
     k0(PLG_K_GATHER);
     launch_gather<D>(st, n, c->perm, c->slot_cell, c->cstart, buf_a<D>(c), buf_b<D>(c), cell_sorted);
@@ -583,6 +586,9 @@ int plg_set_settings(plg_ctx* c, const plg_settings* s) {
         if ((rc = grow(c, &c->cstart, &c->cstart_cap, cells + 1, "cstart"))) return rc;
         const int nparts = scan_blocks((int)cells);
         if ((rc = grow(c, &c->scan_state, &c->scan_cap, (int64_t)nparts + 1, "scan state"))) return rc;
+        // Zero before the first scan on this grid; each step's scatter
+        // zeroes it again after the scan.
+        CK(c, cudaMemset(c->scan_state, 0, sizeof(unsigned long long) * (size_t)(nparts + 1)));
         c->nx = nx;
         c->ncells = (int)cells;
         c->nparts = nparts;

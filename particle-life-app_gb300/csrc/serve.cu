@@ -113,6 +113,7 @@ struct DimState {
     std::vector<ReqPtr> pending;  // in the tail, joining at the next boundary
     std::vector<ReqPtr> leaving;  // retired, download in flight on the side stream
     double busy_s = 0;            // device time of the chunks
+    Clock::time_point last_tune{};
 };
 
 int64_t cells_of(int dim, double rmax) {
@@ -139,7 +140,7 @@ struct plg_server {
     std::string err;
 
     // statistics (under mu)
-    int64_t submitted = 0, completed = 0, compactions = 0;
+    int64_t submitted = 0, completed = 0, compactions = 0, autotunes = 0;
     int64_t resident_bytes = 0, peak_resident_bytes = 0;
     double particle_steps = 0;
     double busy_dim_s[2] = {0, 0};
@@ -277,6 +278,14 @@ bool boundary(plg_server* s, int d, bool* did) {
     int32_t k = 0;
     for (auto& r : S.active) k = std::max(k, r->remaining);
     k = std::min(k, s->cfg.max_chunk_steps);
+    if (k > 0 && s->cfg.autotune_interval_ms > 0 &&
+        ms_between(S.last_tune, Clock::now()) >= (double)s->cfg.autotune_interval_ms) {
+        // Every variant gives the same bits: tuning changes speed only.
+        if (!batch_ok(s, S, plg_batch_autotune_worlds(S.b, 1, nullptr, nullptr), "autotune")) return false;
+        S.last_tune = Clock::now();
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->autotunes++;
+    }
     if (k > 0) {
         if (!cuda_ok(s, cudaEventRecord(S.c0, S.stream), "event")) return false;
         if (!batch_ok(s, S, plg_batch_step_async(S.b, k), "step")) return false;
@@ -561,6 +570,7 @@ int plg_server_stats(plg_server* s, plg_server_stats_t* out) {
     st.busy_dim_s[1] = s->busy_dim_s[1];
     st.busy_s = s->busy_dim_s[0] + s->busy_dim_s[1];
     st.compactions = s->compactions;
+    st.autotunes = s->autotunes;
     st.wall_s = std::chrono::duration<double>(Clock::now() - s->started).count();
     if (!s->latencies_ms.empty()) {
         std::vector<double> v = s->latencies_ms;

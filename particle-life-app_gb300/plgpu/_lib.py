@@ -85,6 +85,7 @@ class plg_server_config(C.Structure):
         ("max_worlds_per_batch", C.c_int32),
         ("max_chunk_steps", C.c_int32),
         ("tile_variant", C.c_int32),
+        ("autotune_interval_ms", C.c_int32),
     ]
 
 
@@ -104,6 +105,7 @@ class plg_server_stats_t(C.Structure):
         ("latency_mean_ms", C.c_double),
         ("busy_dim_s", C.c_double * 2),
         ("compactions", C.c_int64),
+        ("autotunes", C.c_int64),
     ]
 
 
@@ -183,6 +185,10 @@ SIGNATURES = {
     "plg_batch_set_tile": (C.c_int, [_P, C.c_int32]),
     "plg_batch_get_tile": (C.c_int, [_P, _I32P]),
     "plg_batch_autotune": (C.c_int, [_P, C.c_int32, _I32P, _DP]),
+    "plg_batch_autotune_worlds": (C.c_int, [_P, C.c_int32, _I32P, _DP]),
+    "plg_batch_set_world_tile": (C.c_int, [_P, C.c_int32, C.c_int32]),
+    "plg_batch_get_world_tile": (C.c_int, [_P, C.c_int32, _I32P]),
+    "plg_batch_world_ids": (C.c_int, [_P, _I32P]),
     "plg_batch_set_steps": (C.c_int, [_P, C.c_int32, C.c_int32]),
     "plg_batch_steps_left": (C.c_int, [_P, C.c_int32, _I32P]),
     "plg_cursor_count": (C.c_int, [_P, C.POINTER(plg_cursor), _I64P]),

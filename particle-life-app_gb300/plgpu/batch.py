@@ -168,6 +168,33 @@ class GpuBatch:
         _check(self.lib.plg_batch_autotune(self.b, steps, _lib.C.byref(chosen), ms), self.b, "plg_batch_autotune")
         return chosen.value, list(ms)
 
+    def world_ids(self) -> list[int]:
+        """The worlds' ids in device order."""
+        nw = self.counts()[0]
+        ids = np.zeros(max(nw, 1), np.int32)
+        _check(self.lib.plg_batch_world_ids(self.b, _lib.ptr(ids, _lib.C.c_int32)), self.b, "plg_batch_world_ids")
+        return [int(x) for x in ids[:nw]]
+
+    def set_world_tile(self, wid: int, variant: int) -> None:
+        _check(self.lib.plg_batch_set_world_tile(self.b, wid, variant), self.b, "plg_batch_set_world_tile")
+
+    def world_tile(self, wid: int) -> int:
+        v = _lib.C.c_int32()
+        _check(self.lib.plg_batch_get_world_tile(self.b, wid, _lib.C.byref(v)), self.b, "plg_batch_get_world_tile")
+        return v.value
+
+    def autotune_worlds(self, steps: int = 2) -> tuple[dict[int, int], list[float]]:
+        """Gives every world its cheapest tile variant (measured per world;
+        the mix kept only if it beats the best single variant); returns
+        ({world id: variant}, ms per step of each variant alone and of the
+        mix)."""
+        nw = self.counts()[0]
+        var = np.zeros(max(nw, 1), np.int32)
+        ms = (_lib.C.c_double * (_lib.PLG_TILE_VARIANTS + 1))()
+        _check(self.lib.plg_batch_autotune_worlds(self.b, steps, _lib.ptr(var, _lib.C.c_int32), ms), self.b,
+               "plg_batch_autotune_worlds")
+        return dict(zip(self.world_ids(), (int(x) for x in var[:nw]))), list(ms)
+
     def deferred(self) -> int:
         v = _lib.C.c_int64()
         _check(self.lib.plg_batch_step_stats(self.b, _lib.C.byref(v)), self.b, "plg_batch_step_stats")

@@ -59,7 +59,7 @@ def _check(status: int, s, what: str) -> None:
 class Server:
     def __init__(self, memory_budget_bytes: int, particle_capacity=(4_000_000, 4_000_000),
                  cell_capacity=(8_000_000, 8_000_000), max_worlds_per_batch: int = 512, max_chunk_steps: int = 16,
-                 tile_variant: int = 0):
+                 tile_variant: int = 0, autotune_interval_ms: int = 0):
         self.lib = _lib.load()
         cfg = _lib.plg_server_config()
         cfg.memory_budget_bytes = int(memory_budget_bytes)
@@ -68,6 +68,7 @@ class Server:
         cfg.max_worlds_per_batch = max_worlds_per_batch
         cfg.max_chunk_steps = max_chunk_steps
         cfg.tile_variant = tile_variant
+        cfg.autotune_interval_ms = autotune_interval_ms
         h = _lib.C.c_void_p()
         _check(self.lib.plg_server_create(_lib.C.byref(cfg), _lib.C.byref(h)), None, "plg_server_create")
         self.s = h

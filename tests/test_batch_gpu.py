@@ -203,3 +203,45 @@ def test_step_budget_freezes_a_world(gpu):
     for x, y in zip(b.download(ids[1]), ref3[1]):
         assert np.array_equal(x, y)
     b.close()
+
+
+def test_per_world_variants_and_the_per_world_tuner(gpu):
+    """Worlds of one batch on different tile variants give the bits of a
+    uniform batch (a step launches the force kernel once per variant in
+    use); the per-world tuner leaves every world and its step budget where
+    they were, and the batch it tunes continues exactly like an untuned
+    one."""
+    specs = mixed_2d_specs() + [uniform_world(40_000, 5, 0.05, seed=84, vel_scale=0.01)]  # a dense world too
+    b0, ids0 = make_batch(2, specs)
+    b0.set_steps(ids0[2], 2)
+    b0.step(4)
+    ref = [b0.download(w) for w in ids0]
+    b0.close()
+
+    b1, ids1 = make_batch(2, specs)
+    b1.set_steps(ids1[2], 2)
+    for k, w in enumerate(ids1):
+        b1.set_world_tile(w, k % 2)
+    assert [b1.world_tile(w) for w in ids1] == [k % 2 for k in range(len(ids1))]
+    b1.step(4)
+    for w, r in zip(ids1, ref):
+        for a, c in zip(b1.download(w), r):
+            assert np.array_equal(a, c)
+    b1.close()
+
+    b2, ids2 = make_batch(2, specs)
+    b2.set_steps(ids2[2], 2)
+    b2.step(1)
+    before = [b2.download(w) for w in ids2]
+    choice, ms = b2.autotune_worlds(2)
+    assert sorted(choice) == sorted(ids2) and set(choice.values()) <= {0, 1}
+    assert len(ms) == 3 and all(m > 0 for m in ms)
+    assert b2.steps_left(ids2[2]) == 1  # the trials spent no budget
+    for w, r in zip(ids2, before):
+        for a, c in zip(b2.download(w), r):
+            assert np.array_equal(a, c)
+    b2.step(3)
+    for w, r in zip(ids2, ref):
+        for a, c in zip(b2.download(w), r):
+            assert np.array_equal(a, c)
+    b2.close()

@@ -149,7 +149,8 @@ def test_large_worlds_equal_the_world_run_alone(gpu):
 
 def test_generated_requests_and_compaction(gpu):
     """Generated worlds through a server whose batches hold only a few
-    worlds: finished worlds must be compacted away to admit the rest; every
+    worlds and are re-tuned per world at almost every chunk boundary:
+    finished worlds must be compacted away to admit the rest, and every
     result equals plg_generate + plg_step in a single-world context."""
     from plgpu import workloads
     from plgpu.serve import Server
@@ -158,7 +159,7 @@ def test_generated_requests_and_compaction(gpu):
     reqs = [workloads.serving_request_generated(rng, n_lo=2_000, n_hi=30_000, steps_lo=1, steps_hi=20)
             for _ in range(14)]
     srv = Server(memory_budget_bytes=4 << 30, particle_capacity=(70_000, 70_000),
-                 cell_capacity=(2_000_000, 2_000_000), max_chunk_steps=4)
+                 cell_capacity=(2_000_000, 2_000_000), max_chunk_steps=4, autotune_interval_ms=1)
     ids = []
     for dim, g, steps in reqs:
         ids.append(srv.submit_generated(dim, g, steps))
@@ -171,7 +172,7 @@ def test_generated_requests_and_compaction(gpu):
     results = [srv.result(rid) for rid in ids]
     st = srv.stats()
     srv.close()
-    assert st["completed"] == len(ids) and st["compactions"] > 0
+    assert st["completed"] == len(ids) and st["compactions"] > 0 and st["autotunes"] > 0
     assert st["busy_s"] > 0 and st["resident_bytes"] == 0
     for (dim, g, steps), got in zip(reqs, results):
         ref = alone_generated(dim, g, steps)
