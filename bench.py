@@ -688,6 +688,8 @@ def run_ours(args):
 
     peak = _lib.C.c_double()
     check(lib.plg_probe_fp32_peak(_lib.C.byref(peak)), None, "plg_probe_fp32_peak")
+    sfu_peak = _lib.C.c_double()
+    check(lib.plg_probe_sfu_peak(_lib.C.byref(sfu_peak)), None, "plg_probe_sfu_peak")
     peaks = {}
     pk = REPO / "MEASURED_PEAKS.json"
     if pk.exists():
@@ -713,7 +715,12 @@ def run_ours(args):
                 # What actually bounds the kernel: instruction issue (compares,
                 # selects, shared-memory loads and the rsqrt beside the FMAs),
                 # as ncu measured it on this workload.
-                "issue_active_ncu": issue_active}
+                "issue_active_ncu": issue_active,
+                # The special-function unit: one rsqrt per candidate pair,
+                # against an rsqrt.approx microbenchmark run live.
+                "sfu": {"achieved": n * cand / (force_us * 1e-6) / 1e9, "peak": sfu_peak.value, "unit": "Gop/s",
+                        "frac": n * cand / (force_us * 1e-6) / 1e9 / sfu_peak.value,
+                        "work": "one rsqrt.approx per candidate pair"}}
     sort_kernels = {}
     if hbm:
         cells = (int(np.floor(1 / SETTINGS["rmax"]))) ** 2

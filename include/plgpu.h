@@ -343,6 +343,11 @@ int plg_step_stats(plg_ctx* ctx, int64_t* deferred);
  * TFLOP/s (an FFMA counts 2 flops).  Runs for about 0.1 s. */
 int plg_probe_fp32_peak(double* tflops);
 
+/* Device special-function-unit throughput microbenchmark (rsqrt.approx, the
+ * force loop's one SFU operation per candidate pair), in Gop/s.  Runs for
+ * about 0.1 s. */
+int plg_probe_sfu_peak(double* gops);
+
 /* Test hook for the bounded device waits: runs the step's scan kernel on a
  * private two-tile problem where its look-back wait can never be satisfied,
  * so the wait runs out (about 0.3 to 3 s), the kernel raises its error word
@@ -553,12 +558,18 @@ int plg_server_destroy(plg_server* server);
  *   cell_start  device uint32[nx^dim + 1], 16-byte aligned: first slot of
  *               each cell, last = n
  *   status      device uint32 or NULL; the caller zeroes it.  Kernels OR in
- *               1 (a position outside [0,1] or NaN, clamped into the grid)
- *               and 8 (a bounded device wait ran out)
+ *               1 (a position outside [0,1] or NaN: above the box it is
+ *               binned as 1, below it or NaN as 0) and 8 (a bounded device
+ *               wait ran out: cell_start is then not valid).  With NULL
+ *               neither is reported, so a caller that cannot rule out a
+ *               stalled device should pass a status word.
  *   stream      cudaStream_t to enqueue on (NULL: the default stream)
  * Enqueues the work and returns.  n > PLG_NOALLOC_MAX_PARTICLES or
  * nx^dim > PLG_NOALLOC_MAX_CELLS is rejected with PLG_E_CAPACITY, host or
  * other-device pointers with PLG_E_INVALID_ARG, before anything is enqueued.
+ * Cost: linear in n except for crowded cells: the in-cell order takes
+ * n_c^2 / 32 warp steps for a cell of n_c particles (100,000 particles on
+ * one point: about a millisecond; the 2^18 maximum in one cell: several).
  * The first call on a device sets up the scratch address for that device
  * (cudaGetSymbolAddress, which may load the module): make it before any
  * stream capture.  Each call zeroes its own counters on `stream`.  Calls

@@ -271,7 +271,11 @@ __device__ __noinline__ Acc warp_stencil(const ForceArgs<D>& A, const ForceParam
         bool keep = d2 <= P.lo && d2 >= P.tiny;
         bool f64 = false;
         double ddx = 0.0, ddy = 0.0, ddz = 0.0;
-        if (!keep && d2 < P.hi) {
+        // Coincident particles: an FP32 difference is zero exactly when the
+        // FP64 one is (both are exact or rounded once from a multiple of
+        // 2^-149), so the reference's d2 != 0 rejects the pair without FP64.
+        const bool same = dx == 0.f && dy == 0.f && (D == 2 || dz == 0.f);
+        if (!keep && d2 < P.hi && !same) {
             keep = fp64_keeps<D>(P, px, py, pz, q, slmask, ddx, ddy, ddz);
             f64 = d2 < P.tiny;
         }

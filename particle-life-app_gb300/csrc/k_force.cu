@@ -64,7 +64,53 @@ __global__ void __launch_bounds__(256) k_ffma_probe(float* out, int iters, float
     if (r == 12345.678f) out[0] = r;  // keeps the chain live
 }
 
+// The special-function unit: eight independent rsqrt.approx chains per
+// thread (the force loop's one SFU operation per candidate).
+__global__ void __launch_bounds__(256) k_rsqrt_probe(float* out, int iters, float seed) {
+    float a[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) a[k] = seed + threadIdx.x + k;
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int r = 0; r < 16; ++r) {
+#pragma unroll
+            for (int k = 0; k < 8; ++k) asm volatile("rsqrt.approx.ftz.f32 %0, %0;" : "+f"(a[k]));
+        }
+    }
+    float r = 0.f;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) r += a[k];
+    if (r == 12345.678f) out[0] = r;  // keeps the chains live
+}
+
 }  // namespace
+
+cudaError_t probe_sfu_peak(double* gops) {
+    int dev = 0, sms = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+    float* out = nullptr;
+    e = cudaMalloc(&out, sizeof(float));
+    if (e != cudaSuccess) return e;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    const int blocks = sms * 8, threads = 256, iters = 1024;
+    k_rsqrt_probe<<<blocks, threads>>>(out, 16, 1.f);  // warm-up
+    cudaEventRecord(e0);
+    k_rsqrt_probe<<<blocks, threads>>>(out, iters, 1.f);
+    cudaEventRecord(e1);
+    e = cudaEventSynchronize(e1);
+    float ms = 0.f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+    if (e == cudaSuccess) *gops = 8.0 * 16.0 * iters * (double)blocks * threads / (ms * 1e-3) / 1e9;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(out);
+    return e;
+}
 
 cudaError_t probe_fp32_peak(double* tflops) {
     int dev = 0, sms = 0;

@@ -388,5 +388,6 @@ int tile_targets(int dim, int variant);
 cudaError_t force_kernels_init();
 
 cudaError_t probe_fp32_peak(double* tflops);
+cudaError_t probe_sfu_peak(double* gops);
 
 }  // namespace plg

@@ -1404,4 +1404,14 @@ int plg_probe_fp32_peak(double* tflops) {
     return PLG_OK;
 }
 
+int plg_probe_sfu_peak(double* gops) {
+    if (!gops) return PLG_E_INVALID_ARG;
+    const cudaError_t e = probe_sfu_peak(gops);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return PLG_E_CUDA;
+    }
+    return PLG_OK;
+}
+
 }  // extern "C"

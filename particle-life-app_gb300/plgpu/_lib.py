@@ -166,6 +166,7 @@ SIGNATURES = {
     "plg_kernel_name": (C.c_char_p, [C.c_int32]),
     "plg_debug_step": (C.c_int, [_P, _I32P, _I32P, _U64P, _U64P, _FP, _I64P]),
     "plg_probe_fp32_peak": (C.c_int, [_DP]),
+    "plg_probe_sfu_peak": (C.c_int, [_DP]),
     "plg_step_stats": (C.c_int, [_P, _I64P]),
     "plg_sort_cells_noalloc": (C.c_int, [C.c_int32, C.c_double, C.c_int64, _P, _P, _P, _P, _P]),
     "plg_batch_create": (C.c_int, [C.c_int32, C.c_int64, C.c_int32, C.c_int64, C.POINTER(_P)]),

@@ -18,7 +18,8 @@ at a zero of the force (the exact-rmax lattice), where it is ill-conditioned.
 import numpy as np
 import pytest
 
-from worlds import WorldSpec, blob_world, compare_with_oracle, f32, run_gpu_debug, uniform_world
+from worlds import (ACC_TOL, WorldSpec, blob_world, compare_with_oracle, f32, norm_rel, run_gpu_debug,
+                    run_oracle_debug, uniform_world)
 
 pytestmark = pytest.mark.gpu
 
@@ -194,3 +195,55 @@ def test_staged_and_global_memory_paths_agree(gpu, dim):
         b.close()
     for a, c in zip(*runs):
         assert np.array_equal(a, c)
+
+
+def test_crowded_clamp_corner(gpu):
+    """100,000 particles on one point in a corner of a clamped box (the
+    crowded extreme of a clamp-mode world), beside about 20,000 others
+    further than rmax from it: coincident particles do not interact (the
+    reference keeps a pair only when d2 != 0), the corner cell keeps index
+    order, and every other particle steps exactly as in the oracle run
+    without the corner pile (the pile is out of their reach).  The step is
+    timed: the in-cell ordering and the pile's own pair loop grow with the
+    square of its population."""
+    import time
+
+    from plgpu.physics import GpuWorld
+
+    rmax = 0.01
+    others = uniform_world(20_000, 5, rmax, seed=91, vel_scale=0.01, wrap=False)
+    far = np.linalg.norm(others.pos[:, :2], axis=1) > 3 * rmax
+    others = WorldSpec(2, others.pos[far], others.vel[far], others.types[far], others.matrix, rmax, wrap=False)
+    m = others.n
+    pile = 100_000
+    spec = WorldSpec(2, np.concatenate([others.pos, np.zeros((pile, 3))]),
+                     np.concatenate([others.vel, np.zeros((pile, 3))]),
+                     np.concatenate([others.types, np.zeros(pile, np.int32)]), others.matrix, rmax, wrap=False)
+    w = GpuWorld(2, spec.n)
+    w.set_settings(spec.rmax, spec.friction, spec.force, spec.dt, beta=spec.beta, wrap=spec.wrap)
+    w.set_matrix(spec.matrix)
+    w.upload(spec.pos, spec.vel, spec.types)
+    w.step(1)  # warm
+    w.upload(spec.pos, spec.vel, spec.types)
+    t0 = time.perf_counter()
+    w.step(1)
+    dt = time.perf_counter() - t0
+    w.upload(spec.pos, spec.vel, spec.types)
+    g = w.debug_step()
+    gpos, gvel, gtypes, gids = w.download()
+    w.close()
+    print(f"clamp corner pile of {pile:,}: one step {1e3 * dt:.1f} ms")
+    corner = gids >= m
+    assert corner.sum() == pile
+    assert np.all(g["cell"][corner] == 0) and np.all(np.diff(gids[corner]) > 0)  # index order in the cell
+    assert np.all(g["pairs"][corner] == 0) and not g["acc"][corner].any()
+    assert not gpos[corner].any() and not gvel[corner].any()
+    d, o = run_oracle_debug(others)
+    rest = ~corner
+    by_id = np.argsort(gids[rest])
+    oo = np.argsort(o.ids)
+    assert np.array_equal(gids[rest][by_id], o.ids[oo])
+    assert np.array_equal(g["pairs"][rest][by_id], d["pairs"][oo])
+    assert np.array_equal(g["hsum"][rest][by_id], d["hsum"][oo])
+    assert norm_rel(g["acc"][rest][by_id].astype(np.float64), d["acc"][oo]) <= ACC_TOL
+    assert dt < 5.0

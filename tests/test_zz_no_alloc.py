@@ -99,3 +99,66 @@ def test_noalloc_flags_positions_outside_the_box(lib, gpu):
     assert rc == 0
     assert st & 1
     assert np.array_equal(np.sort(perm), np.arange(spec.n)) and cs[-1] == spec.n
+
+
+def _java_order(pos, dim, rmax):
+    """The reference's binning restated on the CPU in FP64: per axis
+    (int)(x / containerSize) with the quotient correctly rounded, cx == nx
+    clamped to nx - 1 (backend/Physics.java:362-375), then a stable counting
+    sort by cell (the sequential fill of Physics.java:342-348).  Positions
+    outside [0, 1] or NaN are clamped as the library clamps them (to 1 above
+    the box, 0 below or NaN)."""
+    nx = int(np.floor(1 / rmax))
+    x = np.nan_to_num(pos[:, :dim], nan=0.0)
+    x = np.where(x > 1.0, 1.0, np.where(x < 0.0, 0.0, x))
+    c = np.minimum((x / rmax).astype(np.int64), nx - 1)
+    cell = c[:, 0] + (c[:, 1] * nx if dim > 1 else 0) + (c[:, 2] * nx * nx if dim > 2 else 0)
+    order = np.argsort(cell, kind="stable")
+    counts = np.bincount(cell, minlength=nx ** dim)
+    return order, np.concatenate([[0], np.cumsum(counts)]), nx ** dim
+
+
+def test_noalloc_fp64_cell_boundaries_against_the_java_rule(lib, gpu):
+    """Double positions one ulp either side of k * rmax (not float32-exact:
+    the FP64 quotient decides their cell), the last partial cell and the box
+    edges, against the CPU restatement of getContainerIndex."""
+    rmax = 0.0031
+    nx = int(np.floor(1 / rmax))
+    rng = np.random.default_rng(25)
+    ks = rng.integers(1, nx + 1, 20_000).astype(np.float64)
+    edge = ks * rmax
+    xs = np.concatenate([np.nextafter(edge, -np.inf), edge, np.nextafter(edge, np.inf), [0.0, 1.0, nx * rmax]])
+    xs = xs[(xs >= 0) & (xs <= 1)]
+    pos = np.zeros((len(xs), 3))
+    pos[:, 0] = xs
+    pos[:, 1] = rng.permutation(np.concatenate([xs[: len(xs) // 2], rng.random(len(xs) - len(xs) // 2)]))
+    order, cstart, ncells = _java_order(pos, 2, rmax)
+    for _ in range(2):
+        rc, perm, cs, st = _noalloc(lib, 2, rmax, pos, len(pos), ncells)
+        assert rc == 0 and st == 0
+        assert np.array_equal(cs, cstart) and np.array_equal(perm, order)
+
+
+def test_noalloc_one_crowded_cell(lib, gpu):
+    """100,000 particles on one point (a corner) among 31,072 others: the
+    crowded cell's members keep index order like every other cell.  The
+    ordering work of a cell grows with the square of its population, shared
+    by the lanes of a warp; this case takes about a millisecond."""
+    import time
+
+    rng = np.random.default_rng(26)
+    n = 131_072
+    pos = np.zeros((n, 3))
+    pos[:, :2] = rng.random((n, 2))
+    crowd = rng.choice(n, 100_000, replace=False)
+    pos[crowd, :2] = 0.0
+    rmax = 0.01
+    order, cstart, ncells = _java_order(pos, 2, rmax)
+    _noalloc(lib, 2, rmax, pos, n, ncells)  # warm
+    t0 = time.perf_counter()
+    rc, perm, cs, st = _noalloc(lib, 2, rmax, pos, n, ncells)
+    dt = time.perf_counter() - t0
+    print(f"crowded cell of 100,000: {1e3 * dt:.2f} ms (call, copies and synchronisation included)")
+    assert rc == 0 and st == 0
+    assert np.array_equal(cs, cstart) and np.array_equal(perm, order)
+    assert dt < 1.0
