@@ -450,7 +450,7 @@ def run_serving(args) -> dict:
     cap = (int(args.serve_cap_2d), int(args.serve_cap_3d))
     cells = (int(args.serve_cells_2d), int(args.serve_cells_3d))
     srv = Server(memory_budget_bytes=150 << 30, particle_capacity=cap, cell_capacity=cells,
-                 max_worlds_per_batch=1024, max_chunk_steps=16, autotune_interval_ms=2000)
+                 max_worlds_per_batch=1024, max_chunk_steps=16, autotune_interval_ms=15000)
     stop = threading.Event()
 
     def collect():  # hands every finished result back to the host and drops it
@@ -521,7 +521,7 @@ def run_serving(args) -> dict:
                       f"{args.serve_drain_s:g} s of drain), 2D/3D 50/50, N log-uniform [1e3, 2e6], types 3..16, "
                       "k U[10, 50], steps U[100, 5000], worlds generated on the device (uniform positions and "
                       f"types, seeded), budget 150 GB, batch capacities {cap[0]:,} (2D) / {cap[1]:,} (3D) "
-                      "particles, chunks of <= 16 steps, per-world tile tuning every 2 s; seeded Philox"}
+                      "particles, chunks of <= 16 steps, per-world tile tuning every 15 s; seeded Philox"}
 
 
 def run_reference(args):
