@@ -447,29 +447,46 @@ struct LoopK {
 // is fma(-1, inv, inv) = +0 exactly, so a candidate beyond rmax adds an exact
 // zero and needs no select.
 template <int D>
-__device__ __forceinline__ float eval_candidate(const LoopK& K, float qx, float qy, float qz, float pxe, float pye,
-                                                float pze, float a, Acc& acc, float& umin) {
-    float dx, dy;
-    sub_pair(qx, qy, pxe, pye, dx, dy);
-    float d2;
-    float dz = 0.f;
+struct Term {
+    float dx, dy, dz, g, d2;
+};
+
+// The term of one candidate (not yet added) and umin = min(umin, |u|).
+template <int D>
+__device__ __forceinline__ Term<D> cand_term(const LoopK& K, float qx, float qy, float qz, float pxe, float pye,
+                                             float pze, float a, float& umin) {
+    Term<D> r;
+    sub_pair(qx, qy, pxe, pye, r.dx, r.dy);
+    r.dz = 0.f;
     if (D == 3) {
-        dz = qz - pze;
-        d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+        r.dz = qz - pze;
+        r.d2 = fmaf(r.dx, r.dx, fmaf(r.dy, r.dy, r.dz * r.dz));
     } else {
-        d2 = fmaf(dx, dx, dy * dy);
+        r.d2 = fmaf(r.dx, r.dx, r.dy * r.dy);
     }
-    const float inv = rsqrt_approx(d2);
-    const float dist = mul_ftz(d2, inv);
+    const float inv = rsqrt_approx(r.d2);
+    const float dist = mul_ftz(r.d2, inv);
     const float t = fmaf(dist, K.m2, K.opb);
     const float u = fmaf(-fabsf(t), K.iomb, 1.f);
     umin = min_nan(umin, fabsf(u));
     const float h = fmaf(a, fmaxf(u, 0.f), -1.f);
-    const float g = fmaf(h, inv, fminf(K.k1, inv));
-    acc.x = fmaf(dx, g, acc.x);
-    acc.y = fmaf(dy, g, acc.y);
-    if (D == 3) acc.z = fmaf(dz, g, acc.z);
-    return d2;
+    r.g = fmaf(h, inv, fminf(K.k1, inv));
+    return r;
+}
+
+template <int D>
+__device__ __forceinline__ void add_term(Acc& acc, const Term<D>& t) {
+    acc.x = fmaf(t.dx, t.g, acc.x);
+    acc.y = fmaf(t.dy, t.g, acc.y);
+    if (D == 3) acc.z = fmaf(t.dz, t.g, acc.z);
+}
+
+template <int D>
+__device__ __forceinline__ float eval_candidate(const LoopK& K, float qx, float qy, float qz, float pxe, float pye,
+                                                float pze, float a, Acc& acc, float& umin) {
+    const Term<D> t = cand_term<D>(K, qx, qy, qz, pxe, pye, pze, a, umin);
+    add_term<D>(acc, t);
+    return t.d2;
 }
 
 // True when the running minimum of |u| asks for the FP64 recomputation.
@@ -508,7 +525,8 @@ __device__ __forceinline__ bool cand_range(const ForceArgs<D>& A, const ForcePar
     const float px1 = px - 1.f, py1 = py - 1.f, pz1 = pz - 1.f;
     float umin = INFINITY;
     const LoopK K(P);
-    for (int j = ja; j < jb; ++j) {
+    // The term of candidate j, with the staged shifts applied.
+    auto term = [&](int j) {
         float4 q = cand[j];
         if (SELF && j == self_j) q.x += 8.f;
         int tb = __float_as_int(D == 3 ? q.w : q.z);
@@ -519,13 +537,32 @@ __device__ __forceinline__ bool cand_range(const ForceArgs<D>& A, const ForcePar
             if (D == 3) pze = (tb & kShiftZ) ? pz1 : pz;
             tb &= 0xffff;
         }
-        const float d2 = eval_candidate<D>(K, q.x, q.y, q.z, pxe, pye, pze, Mrow[tb], acc, umin);
+        return cand_term<D>(K, q.x, q.y, q.z, pxe, pye, pze, Mrow[tb], umin);
+    };
+    auto count = [&](int j, float d2) {
         if (DBG && !(SELF && j == self_j)) {
             acc.cand++;
             if ((d2 <= K.lo) & (d2 > 0.f))
                 add_pair<D, true>(acc, make_float4(0.f, 0.f, 0.f, 0.f),
                                   id_of<D>(A, staged_global(coff, cglob, ncell, j)));
         }
+    };
+    // Two candidates per iteration: their terms are independent chains
+    // (shared-memory load, rsqrt, force law) that overlap in one warp; they
+    // are added in candidate order, so the sum has the same bits as one
+    // candidate at a time.
+    int j = ja;
+    for (; j + 2 <= jb; j += 2) {
+        const Term<D> t0 = term(j), t1 = term(j + 1);
+        add_term<D>(acc, t0);
+        add_term<D>(acc, t1);
+        count(j, t0.d2);
+        count(j + 1, t1.d2);
+    }
+    if (j < jb) {
+        const Term<D> t0 = term(j);
+        add_term<D>(acc, t0);
+        count(j, t0.d2);
     }
     return needs_fp64(K, umin);
 }
