@@ -551,15 +551,18 @@ __device__ __forceinline__ bool cand_range(const ForceArgs<D>& A, const ForcePar
     // (shared-memory load, rsqrt, force law) that overlap in one warp; they
     // are added in candidate order, so the sum has the same bits as one
     // candidate at a time.
+    constexpr int U = D == 3 ? 4 : 2;
     int j = ja;
-    for (; j + 2 <= jb; j += 2) {
-        const Term<D> t0 = term(j), t1 = term(j + 1);
-        add_term<D>(acc, t0);
-        add_term<D>(acc, t1);
-        count(j, t0.d2);
-        count(j + 1, t1.d2);
+    for (; j + U <= jb; j += U) {
+        Term<D> t[U];
+#pragma unroll
+        for (int k = 0; k < U; ++k) t[k] = term(j + k);
+#pragma unroll
+        for (int k = 0; k < U; ++k) add_term<D>(acc, t[k]);
+#pragma unroll
+        for (int k = 0; k < U; ++k) count(j + k, t[k].d2);
     }
-    if (j < jb) {
+    for (; j < jb; ++j) {
         const Term<D> t0 = term(j);
         add_term<D>(acc, t0);
         count(j, t0.d2);
