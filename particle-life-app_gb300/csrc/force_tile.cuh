@@ -141,9 +141,12 @@ __global__ void __launch_bounds__(kThreads) k_force_general(const __grid_constan
 // 2D: variant 0 suits the 1M-particle world (a few cells per tile): 8
 // blocks of 128 targets per SM overlap one block's latency-bound prologue
 // and epilogue with the others' candidate loops better than 4 blocks of
-// 256 (93 vs 95 us per launch, the same 64 registers); variant 1 (fewer
-// blocks, a staging for 2560 candidates) suits very dense worlds (hundreds
-// of particles per cell), where variant 0's windows overflow.
+// 256 (93 vs 95 us per launch, the same 64 registers); variant 1 (4 blocks
+// of 256 targets, a staging for 3072 candidates) suits dense worlds (tens
+// to hundreds of particles per cell), where variant 0's windows overflow.
+// Its few stencil cells per staging keep the block at 52 KB of shared
+// memory, so that 4 fit an SM (with 768 cells and 128 targets only 4 blocks
+// of 4 warps fitted: 15% slower on the batched worlds).
 // 3D: variant 1 is the smaller tile for sparse worlds.
 template <int D, int V>
 struct TileCfg;
@@ -153,7 +156,7 @@ struct TileCfg<2, 0> {
 };
 template <>
 struct TileCfg<2, 1> {
-    static constexpr int kTargets = 128, kMinBlocks = 6, kCap = 2560, kCells = 768;
+    static constexpr int kTargets = 256, kMinBlocks = 4, kCap = 3072, kCells = 192;
 };
 template <>
 struct TileCfg<3, 0> {
