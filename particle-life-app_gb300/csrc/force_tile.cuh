@@ -147,7 +147,12 @@ __global__ void __launch_bounds__(kThreads) k_force_general(const __grid_constan
 // Its few stencil cells per staging keep the block at 52 KB of shared
 // memory, so that 4 fit an SM (with 768 cells and 128 targets only 4 blocks
 // of 4 warps fitted: 15% slower on the batched worlds).
-// 3D: variant 1 is the smaller tile for sparse worlds.
+// 3D: variant 0 (5 blocks of 128 targets at 96 registers) holds 71 staged
+// columns of 9 cells, so that the sparse tails of a blob world stage in one
+// or two rounds, and 2176 candidates for the dense cores (on the 4M-blob
+// world 1.41 ms per launch against 1.49 with 512 cells and 2048 candidates
+// and 1.45 with 384 and 2304; shapes whose shared memory leaves 4 blocks
+// per SM lose 5-10%); variant 1 is the smaller tile for sparse worlds.
 template <int D, int V>
 struct TileCfg;
 template <>
@@ -160,14 +165,14 @@ struct TileCfg<2, 1> {
 };
 template <>
 struct TileCfg<3, 0> {
-    static constexpr int kTargets = 128, kMinBlocks = 5, kCap = 2048, kCells = 512;
+    static constexpr int kTargets = 128, kMinBlocks = 5, kCap = 2176, kCells = 640;
 };
 template <>
 struct TileCfg<3, 1> {
     static constexpr int kTargets = 64, kMinBlocks = 10, kCap = 1024, kCells = 384;
 };
 
-// Lives in dynamic shared memory (variant 0: about 21 KB in 2D, 39 KB in 3D).
+// Lives in dynamic shared memory (variant 0: about 21 KB in 2D, 42 KB in 3D).
 // Staged columns: the sorted union of the windows cx-1..cx+1 of the staged
 // targets, as "virtual" columns -1..nx (-1 and nx being the periodic images
 // of columns nx-1 and 0), each with the grid row of its segment.
