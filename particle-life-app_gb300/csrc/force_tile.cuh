@@ -320,6 +320,7 @@ __global__ void __launch_bounds__(TileCfg<D, V>::kTargets, TileCfg<D, V>::kMinBl
     TileSmem<D, V>& sm = *reinterpret_cast<TileSmem<D, V>*>(smraw);
     const int tid = threadIdx.x;
     pdl_wait();  // the sort before it: B, slot_cell, cstart, the drained counts
+    pdl_release();  // the next step's scan may be scheduled once every block runs
     int wk = 0, s0 = blockIdx.x * kT, nw = A.p.n;
     if (BATCH) {
         wk = world_of(A.tile_off, A.nworlds, blockIdx.x);

@@ -270,6 +270,10 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(const uint32_t* __restric
     __shared__ uint32_t s_tile, s_prefix, total;
     pdl_release();  // the scatter's blocks may be scheduled as this grid ends
     if (threadIdx.x == 0) s_tile = atomicAdd(reinterpret_cast<unsigned int*>(state), 1u);
+    // Launched after the force kernel (launch_scan's `after`), the blocks
+    // may start while it drains: the counts and the deferred-target count
+    // are read or reset only once it has completed.
+    pdl_wait();
     __syncthreads();
     const int tile = (int)s_tile;
     if (tile == 0 && threadIdx.x == 0 && zero_word) *zero_word = 0u;  // the step's deferred-target count
@@ -484,8 +488,12 @@ void launch_download(cudaStream_t st, int n, StateBuf<D> a, double* pos, double*
 int scan_blocks(int ncells) { return blocks_for(ncells, kScanTile); }
 
 void launch_scan(cudaStream_t st, const uint32_t* counts, int ncells, uint32_t* cstart, unsigned long long* state,
-                 uint32_t* status, uint32_t* zero_word) {
-    k_scan<<<scan_blocks(ncells), kScanThreads, 0, st>>>(counts, ncells, cstart, state, status, zero_word);
+                 uint32_t* status, uint32_t* zero_word, bool after) {
+    if (after)
+        launch_after(k_scan, dim3(scan_blocks(ncells)), dim3(kScanThreads), 0, st, counts, ncells, cstart, state,
+                     status, zero_word);
+    else
+        k_scan<<<scan_blocks(ncells), kScanThreads, 0, st>>>(counts, ncells, cstart, state, status, zero_word);
 }
 
 void launch_scatter(cudaStream_t st, int n, const uint32_t* cell, uint32_t* counts, const uint32_t* cstart,

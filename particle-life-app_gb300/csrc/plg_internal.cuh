@@ -322,9 +322,12 @@ void launch_download(cudaStream_t st, int n, StateBuf<D> a, double* pos, double*
 
 int scan_blocks(int ncells);
 // state: (scan_blocks + 1) words, zeroed before each launch; *zero_word is
-// set to 0 (the step's deferred-target count) when not null.
+// set to 0 (the step's deferred-target count) when not null.  after: a
+// programmatic dependent of the kernel before it in `st` (the force kernel
+// of the step before, which releases its dependents once all its blocks
+// run); its blocks wait for that kernel before reading anything it wrote.
 void launch_scan(cudaStream_t st, const uint32_t* counts, int ncells, uint32_t* cstart, unsigned long long* state,
-                 uint32_t* status, uint32_t* zero_word);
+                 uint32_t* status, uint32_t* zero_word, bool after = false);
 // perm[cstart[cell[i]] + r] = i with a rank r taken from counts[cell[i]]
 // (bin_take), which leaves counts at zero for the next counting pass.
 // slot_cell (may be null): receives the cell of each sorted slot.

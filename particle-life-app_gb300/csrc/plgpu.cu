@@ -305,7 +305,8 @@ void enqueue_body(plg_ctx* c, const DebugOut* dbg, int32_t* cell_sorted, const H
     // scatter, and a memset does it.
     const int nstate = c->nparts + 1;
     k0(PLG_K_SCAN);
-    launch_scan(st, c->counts, c->ncells, c->cstart, c->scan_state, c->status_d, c->general ? nullptr : c->defer);
+    launch_scan(st, c->counts, c->ncells, c->cstart, c->scan_state, c->status_d, c->general ? nullptr : c->defer,
+                !c->profiling);
     k1(PLG_K_SCAN);
     k0(PLG_K_SCATTER);
     if (n > 0)
