@@ -422,7 +422,7 @@ int plg_batch_get_stream(plg_batch* batch, void** stream);
 const char* plg_batch_last_error(plg_batch* batch);
 int plg_batch_step_stats(plg_batch* batch, int64_t* deferred);
 /* Force kernel tile variants (threads = targets per block, staging size):
- * 2D: 0 = 128 targets / 1024 staged candidates, 1 = 256 / 3072;
+ * 2D: 0 = 256 targets / 1536 staged candidates, 1 = 256 / 3072;
  * 3D: 0 = 128 / 2176, 1 = 64 / 1024.  Both give the same bits.  Each world
  * of a batch has its own variant; a step launches the force kernel once per
  * variant in use.  The cell size is not a tuning choice: it is rmax (the

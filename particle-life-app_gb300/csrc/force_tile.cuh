@@ -138,15 +138,15 @@ __global__ void __launch_bounds__(kThreads) k_force_general(const __grid_constan
 //               blocks with spilled registers measured slower)
 //   kCap        staged candidates per staging
 //   kCells      stencil cells per staging (R x columns)
-// 2D: variant 0 suits the 1M-particle world (a few cells per tile): 8
-// blocks of 128 targets per SM overlap one block's latency-bound prologue
-// and epilogue with the others' candidate loops better than 4 blocks of
-// 256 (93 vs 95 us per launch, the same 64 registers); variant 1 (4 blocks
-// of 256 targets, a staging for 3072 candidates) suits dense worlds (tens
-// to hundreds of particles per cell), where variant 0's windows overflow.
-// Its few stencil cells per staging keep the block at 52 KB of shared
-// memory, so that 4 fit an SM (with 768 cells and 128 targets only 4 blocks
-// of 4 warps fitted: 15% slower on the batched worlds).
+// 2D: both variants are 4 blocks of 256 targets per SM at 64 registers
+// (32 warps) with 192 stencil cells (64 columns) per staging.  Variant 0
+// stages 1536 candidates (29 KB of shared memory) and suits sparse worlds
+// such as the 1M-particle one (95 us per launch against 97 for 8 blocks of
+// 128 targets with 256 cells); variant 1 stages 3072 (54 KB) for dense
+// worlds (tens to hundreds of particles per cell), where variant 0's
+// windows overflow.  Few stencil cells keep variant 1 at 4 blocks per SM
+// (with 768 cells and 128 targets only 4 blocks of 4 warps fitted: 15%
+// slower on the batched worlds).
 // 3D: variant 0 (5 blocks of 128 targets at 96 registers) holds 71 staged
 // columns of 9 cells, so that the sparse tails of a blob world stage in one
 // or two rounds, and 2176 candidates for the dense cores (on the 4M-blob
@@ -157,7 +157,7 @@ template <int D, int V>
 struct TileCfg;
 template <>
 struct TileCfg<2, 0> {
-    static constexpr int kTargets = 128, kMinBlocks = 8, kCap = 1024, kCells = 256;
+    static constexpr int kTargets = 256, kMinBlocks = 4, kCap = 1536, kCells = 192;
 };
 template <>
 struct TileCfg<2, 1> {
@@ -172,7 +172,7 @@ struct TileCfg<3, 1> {
     static constexpr int kTargets = 64, kMinBlocks = 10, kCap = 1024, kCells = 384;
 };
 
-// Lives in dynamic shared memory (variant 0: about 21 KB in 2D, 42 KB in 3D).
+// Lives in dynamic shared memory (variant 0: about 29 KB in 2D, 42 KB in 3D).
 // Staged columns: the sorted union of the windows cx-1..cx+1 of the staged
 // targets, as "virtual" columns -1..nx (-1 and nx being the periodic images
 // of columns nx-1 and 0), each with the grid row of its segment.

@@ -179,7 +179,7 @@ def test_staged_and_global_memory_paths_agree(gpu, dim):
     from plgpu.batch import GpuBatch, WorldDesc
 
     # 2D: ~220 per cell, a 9-cell window of ~1980 candidates overflows variant
-    # 0's staging (1024) and fits variant 1's (3072).  3D: ~20 per cell, a
+    # 0's staging (1536) and fits variant 1's (3072).  3D: ~20 per cell, a
     # 128-target tile of variant 0 stages whole, variant 1 (1024) in chunks.
     spec = (uniform_world(88_000, 5, 0.05, seed=17, vel_scale=0.01) if dim == 2 else
             uniform_world(20_000, 6, 0.1, seed=18, dim=3, vel_scale=0.01))
