@@ -268,6 +268,7 @@ def run_cfg1(args) -> dict:
     w.set_matrix(m)
     w.upload(pos, vel, types)
     w.step(args.warmup)
+    tile, tile_ms = w.autotune(5)  # untimed; the world is restored
     lib = _lib.load()
     stream = torch.cuda.ExternalStream(w.stream())
     a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -280,6 +281,7 @@ def run_cfg1(args) -> dict:
     w.close()
     return {"metric": "particle-steps/s, 10k 2D (the reference's default world)", "value": n * CFG1["steps"] / (ms * 1e-3),
             "unit": UNIT, "ms_per_step": ms / CFG1["steps"], "steps": CFG1["steps"],
+            "autotune": {"chosen_tile_variant": tile, "ms_per_step_by_variant": tile_ms},
             "config": "2D periodic unit box, N=10,000, 6 types, rmax=0.02 (0.04 in [-1,1]^2), friction t1/2=0.043 s, "
                       "dt=0.02, 1,000 steps (one CUDA graph launch per step); seeded Philox"}
 
@@ -335,8 +337,10 @@ def run_batched(args) -> dict:
                               "how": "each world in its own context, plg_step(K) in turn, host wall clock"},
             "speedup_vs_one_at_a_time": batched / single,
             "autotune": {"per_world": True,
-                         "worlds_by_variant": {str(v): sum(1 for x in choice.values() if x == v) for v in (0, 1)},
-                         "ms_per_step": {"variant_0": tune_ms[0], "variant_1": tune_ms[1], "mixed": tune_ms[2]}},
+                         "worlds_by_variant": {str(v): sum(1 for x in choice.values() if x == v)
+                                               for v in range(len(tune_ms) - 1)},
+                         "ms_per_step": {**{f"variant_{v}": tune_ms[v] for v in range(len(tune_ms) - 1)},
+                                         "mixed": tune_ms[-1]}},
             "config": "512 2D periodic worlds, N log-uniform [1e3, 2e5], types 3..12, rmax U[0.005, 0.03] "
                       "(unit box), friction t1/2 U[0.02, 0.1] s, dt 0.02; seeded Philox"}
 

@@ -422,13 +422,14 @@ int plg_batch_get_stream(plg_batch* batch, void** stream);
 const char* plg_batch_last_error(plg_batch* batch);
 int plg_batch_step_stats(plg_batch* batch, int64_t* deferred);
 /* Force kernel tile variants (threads = targets per block, staging size):
- * 2D: 0 = 256 targets / 1536 staged candidates, 1 = 256 / 3072;
- * 3D: 0 = 128 / 2176, 1 = 64 / 1024.  Both give the same bits.  Each world
+ * 2D: 0 = 256 targets / 1536 staged candidates, 1 = 256 / 3072 (dense
+ * worlds), 2 = 128 / 1024 (small worlds); 3D: 0 = 128 / 2176, 1 = 64 / 1024
+ * (sparse worlds), 2 = 128 / 2816 (dense worlds).  All give the same bits.  Each world
  * of a batch has its own variant; a step launches the force kernel once per
  * variant in use.  The cell size is not a tuning choice: it is rmax (the
  * sorted order the reference exposes depends on it).  A single world has
  * the same choice: plg_set_tile / plg_autotune. */
-#define PLG_TILE_VARIANTS 2
+#define PLG_TILE_VARIANTS 3
 /* Every world (and every world added later) takes `variant`. */
 int plg_batch_set_tile(plg_batch* batch, int32_t variant);
 int plg_batch_get_tile(plg_batch* batch, int32_t* variant);

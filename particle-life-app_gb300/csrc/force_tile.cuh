@@ -153,6 +153,10 @@ __global__ void __launch_bounds__(kThreads) k_force_general(const __grid_constan
 // world 1.41 ms per launch against 1.49 with 512 cells and 2048 candidates
 // and 1.45 with 384 and 2304; shapes whose shared memory leaves 4 blocks
 // per SM lose 5-10%); variant 1 is the smaller tile for sparse worlds.
+// Variant 2: 2D, 8 blocks of 128 targets with 256 cells and 1024 candidates,
+// for small worlds, which the 256-target tiles cut into too few blocks (the
+// 10k-particle world: 40 blocks of 256 on 152 SMs); 3D, 4 blocks of 128
+// targets with 2816 candidates, for dense worlds.
 template <int D, int V>
 struct TileCfg;
 template <>
@@ -164,12 +168,20 @@ struct TileCfg<2, 1> {
     static constexpr int kTargets = 256, kMinBlocks = 4, kCap = 3072, kCells = 192;
 };
 template <>
+struct TileCfg<2, 2> {
+    static constexpr int kTargets = 128, kMinBlocks = 8, kCap = 1024, kCells = 256;
+};
+template <>
 struct TileCfg<3, 0> {
     static constexpr int kTargets = 128, kMinBlocks = 5, kCap = 2176, kCells = 640;
 };
 template <>
 struct TileCfg<3, 1> {
     static constexpr int kTargets = 64, kMinBlocks = 10, kCap = 1024, kCells = 384;
+};
+template <>
+struct TileCfg<3, 2> {
+    static constexpr int kTargets = 128, kMinBlocks = 4, kCap = 2816, kCells = 640;
 };
 
 // Lives in dynamic shared memory (variant 0: about 29 KB in 2D, 42 KB in 3D).
@@ -545,6 +557,8 @@ template <int D, bool DBG, bool BATCH>
 void launch_tile_variant(cudaStream_t st, const ForceArgs<D>& A, bool smem_matrix, int variant, int batch_tiles) {
     if (variant == 1)
         launch_tile<D, DBG, BATCH, 1>(st, A, smem_matrix, batch_tiles);
+    else if (variant == 2)
+        launch_tile<D, DBG, BATCH, 2>(st, A, smem_matrix, batch_tiles);
     else
         launch_tile<D, DBG, BATCH, 0>(st, A, smem_matrix, batch_tiles);
 }

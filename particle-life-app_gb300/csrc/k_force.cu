@@ -12,8 +12,9 @@ namespace plg {
 cudaError_t force_kernels_init_3d();
 
 int tile_targets(int dim, int variant) {
-    if (dim == 2) return variant == 1 ? TileCfg<2, 1>::kTargets : TileCfg<2, 0>::kTargets;
-    return variant == 1 ? TileCfg<3, 1>::kTargets : TileCfg<3, 0>::kTargets;
+    if (dim == 2)
+        return variant == 1 ? TileCfg<2, 1>::kTargets : variant == 2 ? TileCfg<2, 2>::kTargets : TileCfg<2, 0>::kTargets;
+    return variant == 1 ? TileCfg<3, 1>::kTargets : variant == 2 ? TileCfg<3, 2>::kTargets : TileCfg<3, 0>::kTargets;
 }
 
 template void launch_force_batch<2>(cudaStream_t, const ForceParams*, const int*, const int*, const int*, int, int,
@@ -25,7 +26,9 @@ int batch_blocks_per_sm_3d(int variant, bool smem_matrix);
 
 int batch_blocks_per_sm(int dim, int variant, bool smem_matrix) {
     if (dim == 3) return batch_blocks_per_sm_3d(variant, smem_matrix);
-    return variant == 1 ? batch_blocks_per_sm<2, 1>(smem_matrix) : batch_blocks_per_sm<2, 0>(smem_matrix);
+    return variant == 1   ? batch_blocks_per_sm<2, 1>(smem_matrix)
+           : variant == 2 ? batch_blocks_per_sm<2, 2>(smem_matrix)
+                          : batch_blocks_per_sm<2, 0>(smem_matrix);
 }
 
 template void launch_force<2>(cudaStream_t, const ForceParams&, bool, StateBuf<2>, const uint32_t*, const uint32_t*,
@@ -35,6 +38,7 @@ template void launch_force<2>(cudaStream_t, const ForceParams&, bool, StateBuf<2
 cudaError_t force_kernels_init() {
     cudaError_t e = allow_tile_smem<2, 0>();
     if (e == cudaSuccess) e = allow_tile_smem<2, 1>();
+    if (e == cudaSuccess) e = allow_tile_smem<2, 2>();
     if (e == cudaSuccess) e = force_kernels_init_3d();
     return e;
 }

@@ -10,7 +10,9 @@ template void launch_force_batch<3>(cudaStream_t, const ForceParams*, const int*
                                     uint32_t*, uint32_t*, const DebugOut*, int, unsigned long long*);
 
 int batch_blocks_per_sm_3d(int variant, bool smem_matrix) {
-    return variant == 1 ? batch_blocks_per_sm<3, 1>(smem_matrix) : batch_blocks_per_sm<3, 0>(smem_matrix);
+    return variant == 1   ? batch_blocks_per_sm<3, 1>(smem_matrix)
+           : variant == 2 ? batch_blocks_per_sm<3, 2>(smem_matrix)
+                          : batch_blocks_per_sm<3, 0>(smem_matrix);
 }
 
 template void launch_force<3>(cudaStream_t, const ForceParams&, bool, StateBuf<3>, const uint32_t*, const uint32_t*,
@@ -20,6 +22,7 @@ template void launch_force<3>(cudaStream_t, const ForceParams&, bool, StateBuf<3
 cudaError_t force_kernels_init_3d() {
     cudaError_t e = allow_tile_smem<3, 0>();
     if (e == cudaSuccess) e = allow_tile_smem<3, 1>();
+    if (e == cudaSuccess) e = allow_tile_smem<3, 2>();
     return e;
 }
 

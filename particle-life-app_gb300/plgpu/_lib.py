@@ -25,7 +25,7 @@ PLG_E_DEVICE = 8
 PLG_E_CAPACITY = 9
 
 PLG_ACCEL_PARTICLE_LIFE = 1
-PLG_TILE_VARIANTS = 2
+PLG_TILE_VARIANTS = 3
 PLG_NOALLOC_MAX_PARTICLES = 1 << 18
 PLG_NOALLOC_MAX_CELLS = 1 << 18
 

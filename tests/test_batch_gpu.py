@@ -211,6 +211,8 @@ def test_per_world_variants_and_the_per_world_tuner(gpu):
     use); the per-world tuner leaves every world and its step budget where
     they were, and the batch it tunes continues exactly like an untuned
     one."""
+    from plgpu import _lib
+
     specs = mixed_2d_specs() + [uniform_world(40_000, 5, 0.05, seed=84, vel_scale=0.01)]  # a dense world too
     b0, ids0 = make_batch(2, specs)
     b0.set_steps(ids0[2], 2)
@@ -221,8 +223,8 @@ def test_per_world_variants_and_the_per_world_tuner(gpu):
     b1, ids1 = make_batch(2, specs)
     b1.set_steps(ids1[2], 2)
     for k, w in enumerate(ids1):
-        b1.set_world_tile(w, k % 2)
-    assert [b1.world_tile(w) for w in ids1] == [k % 2 for k in range(len(ids1))]
+        b1.set_world_tile(w, k % _lib.PLG_TILE_VARIANTS)
+    assert [b1.world_tile(w) for w in ids1] == [k % _lib.PLG_TILE_VARIANTS for k in range(len(ids1))]
     b1.step(4)
     for w, r in zip(ids1, ref):
         for a, c in zip(b1.download(w), r):
@@ -234,8 +236,8 @@ def test_per_world_variants_and_the_per_world_tuner(gpu):
     b2.step(1)
     before = [b2.download(w) for w in ids2]
     choice, ms = b2.autotune_worlds(2)
-    assert sorted(choice) == sorted(ids2) and set(choice.values()) <= {0, 1}
-    assert len(ms) == 3 and all(m > 0 for m in ms)
+    assert sorted(choice) == sorted(ids2) and set(choice.values()) <= set(range(_lib.PLG_TILE_VARIANTS))
+    assert len(ms) == _lib.PLG_TILE_VARIANTS + 1 and all(m > 0 for m in ms)
     assert b2.steps_left(ids2[2]) == 1  # the trials spent no budget
     for w, r in zip(ids2, before):
         for a, c in zip(b2.download(w), r):
