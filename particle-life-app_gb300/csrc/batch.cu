@@ -55,6 +55,12 @@ struct plg_batch {
     int64_t pcap = 0, ccap = 0;
     int32_t wcap = 0;
     cudaStream_t stream = nullptr;
+    // Force launches of the variants after the first one in use run on
+    // streams of their own (forked from and joined back into `stream`), so
+    // that one variant's last wave overlaps the others' blocks.
+    cudaStream_t vstream[PLG_TILE_VARIANTS] = {};
+    cudaEvent_t vfork = nullptr;
+    cudaEvent_t vjoin[PLG_TILE_VARIANTS] = {};
 
     float4* apt = nullptr;
     float4* bpt = nullptr;
@@ -205,6 +211,11 @@ void free_batch(plg_batch* b) {
     for (void* p : b->tune_save)
         if (p) cudaFree(p);
     if (b->status_h) cudaFreeHost(b->status_h);
+    for (int v = 0; v < PLG_TILE_VARIANTS; ++v) {
+        if (b->vstream[v]) cudaStreamDestroy(b->vstream[v]);
+        if (b->vjoin[v]) cudaEventDestroy(b->vjoin[v]);
+    }
+    if (b->vfork) cudaEventDestroy(b->vfork);
     if (b->stream) cudaStreamDestroy(b->stream);
 }
 
@@ -478,12 +489,32 @@ void enqueue_batch_step(plg_batch* b, const DebugOut* dbg, int32_t* cell_sorted,
     launch_gather<D>(st, n, b->perm, b->slot_cell, b->cstart, sbuf<D>(b->apt, b->avel, 0),
                      sbuf<D>(b->bpt, b->bvel, 0), cell_sorted);
     // One force launch per tile variant in use; the launches touch disjoint
-    // worlds.
-    for (int v = 0; v < PLG_TILE_VARIANTS; ++v)
-        launch_force_batch<D>(st, b->worlds_d, b->wp_off_d, b->tile_off_d + (size_t)v * (b->wcap + 1),
+    // worlds (their shared outputs, the next counts and the deferred count,
+    // are atomics).  The first runs on the step's stream after the gather,
+    // the others concurrently on their own streams, joined before the tick.
+    auto force = [&](cudaStream_t s, int v) {
+        launch_force_batch<D>(s, b->worlds_d, b->wp_off_d, b->tile_off_d + (size_t)v * (b->wcap + 1),
                               b->steps_left_d, b->tiles[v], (int)b->worlds.size(), n, b->smem_matrix,
                               sbuf<D>(b->bpt, b->bvel, 0), b->cstart, b->slot_cell, sbuf<D>(b->apt, b->avel, 0),
                               b->cell, b->counts, b->defer, dbg, v, wcycles);
+    };
+    int first = -1;
+    for (int v = 0; v < PLG_TILE_VARIANTS; ++v)
+        if (b->tiles[v] > 0 && first < 0) first = v;
+    bool forked = false;
+    for (int v = first + 1; first >= 0 && v < PLG_TILE_VARIANTS; ++v) {
+        if (b->tiles[v] <= 0) continue;
+        if (!forked) {
+            cudaEventRecord(b->vfork, st);
+            forked = true;
+        }
+        cudaStreamWaitEvent(b->vstream[v], b->vfork, 0);
+        force(b->vstream[v], v);
+        cudaEventRecord(b->vjoin[v], b->vstream[v]);
+    }
+    if (first >= 0) force(st, first);
+    for (int v = first + 1; forked && v < PLG_TILE_VARIANTS; ++v)
+        if (b->tiles[v] > 0) cudaStreamWaitEvent(st, b->vjoin[v], 0);
     launch_batch_tick(st, b->steps_left_d, (int)b->worlds.size());
 }
 
@@ -844,6 +875,11 @@ int plg_batch_create(int32_t dim, int64_t particle_capacity, int32_t world_capac
         }
     };
     if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess) rc = PLG_E_CUDA;
+    if (!rc && cudaEventCreateWithFlags(&b->vfork, cudaEventDisableTiming) != cudaSuccess) rc = PLG_E_CUDA;
+    for (int v = 0; v < PLG_TILE_VARIANTS && !rc; ++v)
+        if (cudaStreamCreateWithFlags(&b->vstream[v], cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&b->vjoin[v], cudaEventDisableTiming) != cudaSuccess)
+            rc = PLG_E_CUDA;
     if (!rc && force_kernels_init() != cudaSuccess) rc = PLG_E_CUDA;
     const size_t pc = (size_t)particle_capacity, cc = (size_t)cell_capacity, wc = (size_t)world_capacity;
     const size_t vel_sz = dim == 2 ? sizeof(float2) : sizeof(float4);
