@@ -78,7 +78,7 @@ struct plg_batch {
 
     ForceParams* worlds_d = nullptr;  // wcap
     int* wp_off_d = nullptr;          // wcap + 1
-    int* tile_off_d = nullptr;        // PLG_TILE_VARIANTS x (wcap + 1): first tile of each world
+    int* tile_off_d = nullptr;        // PLG_TILE_VARIANTS x (2 wcap + 1): tile layout of each launch
     int* steps_left_d = nullptr;      // wcap: device countdown, a world at 0 is frozen
     int tiles[PLG_TILE_VARIANTS] = {};
     int* move_new_d = nullptr;        // wcap + 1
@@ -282,17 +282,37 @@ int check_desc(plg_batch* b, const plg_world_desc& d) {
 // every world in the launch of v's worlds (a world of another variant has
 // no tiles there).  A block never spans two worlds, and every world is cut
 // into exactly the tiles a single-world launch of its variant uses.
+size_t tile_stride(const plg_batch* b) { return 2 * (size_t)b->wcap + 1; }
+
+// Tile layout of each variant's launch: its worlds in decreasing order of
+// particles per cell (longest blocks first, so that the launch does not end
+// on a straggling dense tile), then the rest with no tiles.
 int write_tiles(plg_batch* b) {
     const size_t nw = b->worlds.size();
-    std::vector<int> toff((size_t)PLG_TILE_VARIANTS * (b->wcap + 1), 0);
+    const size_t stride = tile_stride(b);
+    std::vector<int> toff((size_t)PLG_TILE_VARIANTS * stride, 0);
+    std::vector<int> order(nw);
+    auto density = [&](size_t k) {
+        const WorldRec& w = b->worlds[k];
+        return w.dead ? 0.0 : (double)w.n / (double)std::max<int64_t>(w.ncells, 1);
+    };
     for (int v = 0; v < PLG_TILE_VARIANTS; ++v) {
         const int kt = tile_targets(b->dim, v);
+        for (size_t k = 0; k < nw; ++k) order[k] = (int)k;
+        std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+            const bool ix = b->worlds[x].variant == v, iy = b->worlds[y].variant == v;
+            if (ix != iy) return ix;
+            return ix && density(x) > density(y);
+        });
+        int* off = toff.data() + (size_t)v * stride;
         int t = 0;
-        for (size_t k = 0; k < nw; ++k) {
-            toff[(size_t)v * (b->wcap + 1) + k] = t;
+        for (size_t q = 0; q < nw; ++q) {
+            const int k = order[q];
+            off[q] = t;
+            off[nw + 1 + q] = k;
             if (b->worlds[k].variant == v) t += (int)((b->worlds[k].n + kt - 1) / kt);
         }
-        toff[(size_t)v * (b->wcap + 1) + nw] = t;
+        off[nw] = t;
         b->tiles[v] = t;
     }
     BCK(b, cudaMemcpyAsync(b->tile_off_d, toff.data(), sizeof(int) * toff.size(), cudaMemcpyHostToDevice, b->stream));
@@ -493,7 +513,7 @@ void enqueue_batch_step(plg_batch* b, const DebugOut* dbg, int32_t* cell_sorted,
     // are atomics).  The first runs on the step's stream after the gather,
     // the others concurrently on their own streams, joined before the tick.
     auto force = [&](cudaStream_t s, int v) {
-        launch_force_batch<D>(s, b->worlds_d, b->wp_off_d, b->tile_off_d + (size_t)v * (b->wcap + 1),
+        launch_force_batch<D>(s, b->worlds_d, b->wp_off_d, b->tile_off_d + (size_t)v * tile_stride(b),
                               b->steps_left_d, b->tiles[v], (int)b->worlds.size(), n, b->smem_matrix,
                               sbuf<D>(b->bpt, b->bvel, 0), b->cstart, b->slot_cell, sbuf<D>(b->apt, b->avel, 0),
                               b->cell, b->counts, b->defer, dbg, v, wcycles);
@@ -897,7 +917,7 @@ int plg_batch_create(int32_t dim, int64_t particle_capacity, int32_t world_capac
     dm((void**)&b->status_d, 64);
     dm((void**)&b->worlds_d, sizeof(ForceParams) * wc);
     dm((void**)&b->wp_off_d, sizeof(int) * (wc + 1));
-    dm((void**)&b->tile_off_d, sizeof(int) * PLG_TILE_VARIANTS * (wc + 1));
+    dm((void**)&b->tile_off_d, sizeof(int) * PLG_TILE_VARIANTS * (2 * wc + 1));
     dm((void**)&b->steps_left_d, sizeof(int) * wc);
     dm((void**)&b->move_new_d, sizeof(int) * (wc + 1));
     dm((void**)&b->move_old_d, sizeof(int) * wc);

@@ -28,8 +28,10 @@ struct ForceArgs {
     DebugOut dbg;
     HostSnap snap;  // snapshot arrays written by the tiled kernel's SNAP form
     // Batched worlds: per-world parameters, first sorted slots
-    // (wp_off[k] = worlds[k].p_off) and first tiles (tile_off[k] = the sum
-    // of ceil(n_j / kTargets) over j < k), nworlds + 1 entries each.
+    // (wp_off[k] = worlds[k].p_off, nworlds + 1 entries) and the launch's
+    // tile layout: tile_off[q] (q = 0 .. nworlds) is the first tile of the
+    // q-th world in launch order and tile_off[nworlds + 1 + q] that world's
+    // index (worlds with no tiles in this launch take none).
     const ForceParams* __restrict__ worlds;
     const int* __restrict__ wp_off;
     const int* __restrict__ tile_off;

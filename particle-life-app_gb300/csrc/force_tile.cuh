@@ -335,8 +335,9 @@ __global__ void __launch_bounds__(TileCfg<D, V>::kTargets, TileCfg<D, V>::kMinBl
     pdl_release();  // the next step's scan may be scheduled once every block runs
     int wk = 0, s0 = blockIdx.x * kT, nw = A.p.n;
     if (BATCH) {
-        wk = world_of(A.tile_off, A.nworlds, blockIdx.x);
-        const int t = blockIdx.x - __ldg(A.tile_off + wk);
+        const int q = world_of(A.tile_off, A.nworlds, blockIdx.x);
+        wk = __ldg(A.tile_off + A.nworlds + 1 + q);
+        const int t = blockIdx.x - __ldg(A.tile_off + q);
         s0 = __ldg(A.wp_off + wk) + t * kT;
         nw = __ldg(A.wp_off + wk + 1) - s0;  // targets of this world from s0 on
     } else {
