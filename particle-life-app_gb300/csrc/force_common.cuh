@@ -355,6 +355,12 @@ struct TileRows {
 // the target uses x - 1 (y - 1, z - 1) against it, because the candidate is
 // the periodic image above the box of a cell near coordinate 0.
 constexpr int kShiftX = 1 << 16, kShiftY = 1 << 17, kShiftZ = 1 << 18;
+// Staging only (never in a staged word): the cell's image lies below the box
+// in x or y and its candidates are shifted down by 1 as they are copied.
+constexpr int kNegX = 1 << 20, kNegY = 1 << 21;
+// Average staged candidates per cell from which a 2D block copies its cells
+// one warp per cell instead of one owner thread per cell.
+constexpr int kDenseCell = 16;
 
 __device__ __forceinline__ int wrap_index(int c, int n) { return c < 0 ? c + n : (c >= n ? c - n : c); }
 

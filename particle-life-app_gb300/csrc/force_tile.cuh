@@ -194,6 +194,7 @@ struct TileSmem {
     float4 cand[TileCfg<D, V>::kCap];      // staged candidates, column-major by stencil cell
     int coff[TileCfg<D, V>::kCells + 1];   // smem start of stencil cell e = column * R + row
     int cglob[TileCfg<D, V>::kCells];      // sorted-order start of stencil cell e
+    int cshift[D == 2 ? TileCfg<D, V>::kCells : 1];  // 2D dense staging: image shifts of cell e (kShift*, kNeg*)
     int colv[kCols];                       // virtual column of staged column ci
     int colrow[kCols];                     // grid row (y, or y + z nx) of staged column ci
     int rowid[TileCfg<D, V>::kTargets];
@@ -259,6 +260,12 @@ __device__ __forceinline__ bool stage_columns(const ForceArgs<D>& A, const Force
         total += x;
     }
     if (total > TileCfg<D, V>::kCap) return false;  // block-uniform
+    // 2D windows of kDenseCell or more candidates per cell on average: each
+    // cell is copied by one warp (its lanes take every 32nd member), so that
+    // a crowded cell does not hold the block at the barrier behind a single
+    // thread; the owners only publish their cells' shifts.  Sparse windows:
+    // each owner thread copies its cells.  The same slots either way.
+    const bool dense = D == 2 && total >= kDenseCell * ncell;  // block-uniform
     int run = before + inc - sum;
 #pragma unroll
     for (int i = 0; i < kPer; ++i) {
@@ -284,20 +291,34 @@ __device__ __forceinline__ bool stage_columns(const ForceArgs<D>& A, const Force
                     if (cz + oz >= nx) flags |= kShiftZ;
                 }
             }
-            const float4* __restrict__ src = A.bpt + g0[i];
-            float4* dst = sm.cand + run;
-            const int m = len[i];
-            int k = 0;
-            for (; k + 4 <= m; k += 4) {
-                float4 q[4];
+            if (D == 2 && dense) {
+                sm.cshift[e] = flags | (sx != 0.f ? kNegX : 0) | (sy != 0.f ? kNegY : 0);
+            } else {
+                const float4* __restrict__ src = A.bpt + g0[i];
+                float4* dst = sm.cand + run;
+                const int m = len[i];
+                int k = 0;
+                for (; k + 4 <= m; k += 4) {
+                    float4 q[4];
 #pragma unroll
-                for (int u = 0; u < 4; ++u) q[u] = __ldg(src + k + u);
+                    for (int u = 0; u < 4; ++u) q[u] = __ldg(src + k + u);
 #pragma unroll
-                for (int u = 0; u < 4; ++u) dst[k + u] = shift_candidate<D>(q[u], sx, sy, sz, flags);
+                    for (int u = 0; u < 4; ++u) dst[k + u] = shift_candidate<D>(q[u], sx, sy, sz, flags);
+                }
+                for (; k < m; ++k) dst[k] = shift_candidate<D>(__ldg(src + k), sx, sy, sz, flags);
             }
-            for (; k < m; ++k) dst[k] = shift_candidate<D>(__ldg(src + k), sx, sy, sz, flags);
         }
         run += len[i];
+    }
+    if (D == 2 && dense) {
+        __syncthreads();
+        for (int e = warp; e < ncell; e += kT / 32) {
+            const int d = sm.coff[e], m = sm.coff[e + 1] - d, f = sm.cshift[e];
+            const float4* __restrict__ src = A.bpt + sm.cglob[e];
+            const float sx = (f & kNegX) ? 1.f : 0.f, sy = (f & kNegY) ? 1.f : 0.f;
+            for (int k = lane; k < m; k += 32)
+                sm.cand[d + k] = shift_candidate<D>(__ldg(src + k), sx, sy, 0.f, f & (kShiftX | kShiftY));
+        }
     }
     __syncthreads();
     return true;
