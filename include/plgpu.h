@@ -299,8 +299,10 @@ int plg_set_use_graph(plg_ctx* ctx, int32_t on);
 #define PLG_K_FORCE 3   /* neighbour loop + integration + counting */
 #define PLG_K_COUNT 4
 
-/* Force kernel tile variant of this world (see PLG_TILE_VARIANTS below; 0
- * by default).  Every variant gives the same bits. */
+/* Force kernel tile variant of this world (see PLG_TILE_VARIANTS below).
+ * Until plg_set_tile or plg_autotune chooses one, 2D worlds under 300,000
+ * particles use variant 2 and all others variant 0.  Every variant gives
+ * the same bits. */
 int plg_set_tile(plg_ctx* ctx, int32_t variant);
 int plg_get_tile(plg_ctx* ctx, int32_t* variant);
 /* Times `steps` steps of every tile variant on the world as it is

@@ -143,26 +143,29 @@ def test_batch_rejects_what_it_cannot_run(gpu):
 
 
 def test_autotune_restores_state_and_variants_agree(gpu):
+    from plgpu import _lib
+
     specs = mixed_2d_specs()[:4]
     b, ids = make_batch(2, specs)
     b.step(2)
     before = [b.download(w) for w in ids]
     v, ms = b.autotune(2)
-    assert v == b.tile() and v in (0, 1) and all(m > 0 for m in ms)
+    assert v == b.tile() and v in range(_lib.PLG_TILE_VARIANTS) and all(m > 0 for m in ms)
     for w, ref in zip(ids, before):
         for x, y in zip(b.download(w), ref):
             assert np.array_equal(x, y)
     b.close()
     runs = []
-    for variant in (0, 1):
+    for variant in range(_lib.PLG_TILE_VARIANTS):
         bb, ii = make_batch(2, specs)
         bb.set_tile(variant)
         bb.step(4)
         runs.append([bb.download(w) for w in ii])
         bb.close()
-    for r0, r1 in zip(*runs):  # tile variants give the same bits
-        for a, c in zip(r0, r1):
-            assert np.array_equal(a, c)
+    for other in runs[1:]:  # tile variants give the same bits
+        for r0, r1 in zip(runs[0], other):
+            for a, c in zip(r0, r1):
+                assert np.array_equal(a, c)
 
 
 def test_dense_world_alone_and_in_a_mix_is_bit_identical(gpu):
