@@ -197,8 +197,6 @@ struct TileSmem {
     int cshift[D == 2 ? TileCfg<D, V>::kCells : 1];  // 2D dense staging: image shifts of cell e (kShift*, kNeg*)
     int colv[kCols];                       // virtual column of staged column ci
     int colrow[kCols];                     // grid row (y, or y + z nx) of staged column ci
-    int rowid[TileCfg<D, V>::kTargets];
-    int colid[TileCfg<D, V>::kTargets];
     int wsum[TileCfg<D, V>::kTargets / 32];
     int wcol[TileCfg<D, V>::kTargets / 32];
     float mat[kSmemMatrixMax * smem_matrix_stride<D>(kSmemMatrixMax)];
@@ -389,29 +387,38 @@ __global__ void __launch_bounds__(TileCfg<D, V>::kTargets, TileCfg<D, V>::kMinBl
     const float* M = SMEM_M ? sm.mat : P.matrix;
     float4 me = make_float4(0.f, 0.f, 0.f, 0.f);
     typename Layout<D>::Vel vme{};
-    int cx = 0, row = INT_MAX;
+    const int lane = tid & 31, warp = tid >> 5;
+    int cx = 0, row = INT_MAX, prow = INT_MAX, pcx = 0;
     if (valid) {
         // The target's cell is the one the sort binned it by (computed from
         // these same coordinates by the previous epilogue or the upload).
+        // The first lane of a warp also reads the cell of the target before
+        // it (the other lanes take their neighbour's by a shuffle).
         const uint32_t c = __ldg(A.slot_cell + s) - P.cell_base;
+        const uint32_t cp = lane == 0 && tid > 0 ? __ldg(A.slot_cell + s - 1) - P.cell_base : 0u;
         me = A.bpt[s];
         vme = A.bvel[s];  // needed only by the epilogue: loaded early, off its critical path
         const uint32_t nxu = (uint32_t)P.g.nx;
         row = (int)(c / nxu);
         cx = (int)(c - (uint32_t)row * nxu);
+        prow = (int)(cp / nxu);
+        pcx = (int)(cp - (uint32_t)prow * nxu);
     }
-    sm.rowid[tid] = row;
-    sm.colid[tid] = cx;
-    __syncthreads();
     // Segments: maximal runs of targets in one grid row (rows are
     // nondecreasing, and so are the columns within a segment).  Window
     // columns: each first target of a column adds the columns of its window
     // cx-1..cx+1 that the previous column's window has not added (3 at a
     // segment start); a block-wide scan numbers them, so the target's window
     // starts at staged column kwin = incl - 3.
-    const int lane = tid & 31, warp = tid >> 5;
-    const int pcol = tid > 0 ? sm.colid[tid - 1] : 0;
-    const bool start = valid && (tid == 0 || sm.rowid[tid - 1] != row);
+    {
+        const int r_up = __shfl_up_sync(kFull, row, 1), c_up = __shfl_up_sync(kFull, cx, 1);
+        if (lane > 0) {
+            prow = r_up;
+            pcx = c_up;
+        }
+    }
+    const int pcol = tid > 0 ? pcx : 0;
+    const bool start = valid && (tid == 0 || prow != row);
     const bool lead = valid && (start || pcol != cx);
     const int newc = !lead ? 0 : (start ? 3 : min(3, cx - pcol));
     int incl = newc;
