@@ -140,9 +140,9 @@ __global__ void __launch_bounds__(kThreads) k_force_general(const __grid_constan
 //   kCells      stencil cells per staging (R x columns)
 // 2D: both variants are 4 blocks of 256 targets per SM at 64 registers
 // (32 warps) with 192 stencil cells (64 columns) per staging.  Variant 0
-// stages 1536 candidates (29 KB of shared memory) and suits sparse worlds
+// stages 1536 candidates (28 KB of shared memory) and suits sparse worlds
 // such as the 1M-particle one (95 us per launch against 97 for 8 blocks of
-// 128 targets with 256 cells); variant 1 stages 3072 (54 KB) for dense
+// 128 targets with 256 cells); variant 1 stages 3072 (53 KB) for dense
 // worlds (tens to hundreds of particles per cell), where variant 0's
 // windows overflow.  Few stencil cells keep variant 1 at 4 blocks per SM
 // (with 768 cells and 128 targets only 4 blocks of 4 warps fitted: 15%
@@ -184,7 +184,7 @@ struct TileCfg<3, 2> {
     static constexpr int kTargets = 128, kMinBlocks = 4, kCap = 2816, kCells = 640;
 };
 
-// Lives in dynamic shared memory (variant 0: about 29 KB in 2D, 42 KB in 3D).
+// Lives in dynamic shared memory (variant 0: about 28 KB in 2D, 42 KB in 3D).
 // Staged columns: the sorted union of the windows cx-1..cx+1 of the staged
 // targets, as "virtual" columns -1..nx (-1 and nx being the periodic images
 // of columns nx-1 and 0), each with the grid row of its segment.
