@@ -63,13 +63,14 @@ def test_autotune_restores_the_world(gpu, case):
     try:
         a.step(1)
         b.step(1)
+        before = a.tile()
         chosen, ms = a.autotune(3)
         assert chosen in range(_lib.PLG_TILE_VARIANTS)
         assert a.tile() == chosen
         assert len(ms) == _lib.PLG_TILE_VARIANTS and all(t > 0 for t in ms)
         fastest = int(np.argmin(ms))
-        # the fastest variant replaces the current one (0) only when it is at least 2% faster
-        assert chosen == (fastest if ms[fastest] < 0.98 * ms[0] else 0)
+        # the fastest variant replaces the current one only when it is at least 2% faster
+        assert chosen == (fastest if ms[fastest] < 0.98 * ms[before] else before)
         for x, y in zip(a.download(), b.download()):
             assert np.array_equal(x, y)
         a.step(2)
@@ -101,3 +102,21 @@ def test_tile_errors_and_small_grid(gpu):
         assert fresh.lib.plg_autotune(fresh.ctx, 2, _lib.C.byref(c), None) == _lib.PLG_E_STATE  # not ready
     finally:
         fresh.close()
+
+
+def test_default_variant_follows_the_size(gpu):
+    """Until a variant is set or tuned, 2D worlds under 300,000 particles
+    take the 128-target tile (variant 2) and larger ones variant 0; 3D
+    worlds variant 0.  Setting a variant overrides the default."""
+    small, large = uniform_world(10_000, 6, 0.02, seed=71), uniform_world(400_000, 6, 0.004, seed=72)
+    small3 = uniform_world(20_000, 6, 0.05, seed=73, dim=3)
+    worlds = [_world(small), _world(large), _world(small3)]
+    try:
+        assert [w.tile() for w in worlds] == [2, 0, 0]
+        worlds[0].set_tile(1)
+        assert worlds[0].tile() == 1
+        worlds[0].step(1)
+        assert worlds[0].tile() == 1
+    finally:
+        for w in worlds:
+            w.close()
